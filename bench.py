@@ -1,0 +1,364 @@
+"""Benchmark: histories/s of the Monte Carlo k-eigenvalue generation loop.
+
+Workload (default): single_large — 1D fuel/water slab, 4 groups, 2,000 tally
+cells, 1M histories per generation, fission-bank power iteration; a step is
+one generation.  Warm-up steps are the inactive generations, timed steps the
+active ones (defaults 50 + 200, the full workload), so sigma_k of the timed
+generations is reported beside the throughput.
+
+Arms:
+  default            the chosen form (event-based Woodcock, FP32 flights, FP64
+                     tallies/k), falling back to nothing: if the CUDA library
+                     cannot run, the bench fails.
+  --impl reference   the reference algorithm (CPU restatement of
+                     src/mc_code.rs in COMPAT mode, f32, the reference's thread
+                     policy T = cores - 1) on a bounded sample per step.
+
+Timing: every step is bracketed by CUDA events on the engine's stream; the L2
+(129 MB) is flushed between steps by writing a 256 MB buffer outside the
+brackets.  `e2e` times the drop-in C-ABI call nraps_monte_carlo with host
+buffers on the whole workload.  One JSON line is printed by rank 0.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+ALG_BYTES_PER_COLLISION = 48  # 24 B particle record read + written per real collision
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        d = json.load(open(path))
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def traffic_per_collision():
+    """DRAM bytes per real collision of the dominant kernel from the committed
+    ncu summary (profiles/*traffic*.txt: 'bytes_per_collision = X'), or None."""
+    d = os.path.join(ROOT, "profiles")
+    if not os.path.isdir(d):
+        return None
+    for f in sorted(os.listdir(d)):
+        if "traffic" in f and f.endswith(".txt"):
+            for line in open(os.path.join(d, f)):
+                if line.strip().startswith("bytes_per_collision"):
+                    try:
+                        return float(line.split("=")[1])
+                    except ValueError:
+                        pass
+    return None
+
+
+class Clocks:
+    def __init__(self, index: int):
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(index), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.fh.close()
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = max(mx, float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return None
+        loaded = [v for v in sm if v > 0.5 * max(sm)] or sm
+        return {"sm_mhz": statistics.median(loaded), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def make_workload(name: str, seed: int, warmup: int, steps: int):
+    from nraps_gb300 import synth
+    if name == "single_large":
+        p = synth.single_large(seed)
+    elif name == "plain_small":
+        p = synth.plain_small(seed)
+    elif name == "scale_stress":
+        p = synth.scale_stress(seed)
+    else:
+        raise SystemExit(f"unknown workload {name}")
+    p = p.with_(generations=warmup + steps, skip=warmup)
+    return p
+
+
+ARMS = {
+    "event": dict(mode=2, precision=1, tracking=1),
+    "plain": dict(mode=2, precision=0, tracking=0),
+}
+
+
+def measure_device(prob, arm: str, steps: int, warmup: int, seed: int, device: int):
+    """Device-resident throughput: per-step CUDA events on the engine stream."""
+    import torch
+    from nraps_gb300 import api
+    ctx = api.Context(seed=seed, device=device, **ARMS[arm])
+    s = ctx.session(prob)
+    s.set_profile(True)
+    ext = torch.cuda.ExternalStream(ctx.stream_ptr, device=device)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{device}")
+    s.run(warmup)
+    t0 = s.timing()
+    launches0 = ctx.launches
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    torch.cuda.synchronize(device)
+    for i in range(steps):
+        with torch.cuda.stream(ext):
+            flush.zero_()
+            ev[i][0].record(ext)
+        s.run(1)
+        with torch.cuda.stream(ext):
+            ev[i][1].record(ext)
+    torch.cuda.synchronize(device)
+    t1 = s.timing()
+    ms = sum(a.elapsed_time(b) for a, b in ev)
+    res = s.results()
+    out = dict(ms=ms, histories=steps * prob.histories, collisions=t1["collisions"] - t0["collisions"],
+               transport_ms=t1["transport_ms"] - t0["transport_ms"],
+               transport_launches=t1["transport_launches"] - t0["transport_launches"],
+               launches=ctx.launches - launches0 - 0, k_mean=res.stats.k_mean, k_sigma=res.stats.k_sigma)
+    # the flush zero_() launches are torch's, not ours; ctx.launches counts ours
+    s.close()
+    ctx.close()
+    del flush
+    return out
+
+
+def measure_e2e(prob, arm: str, seed: int, device: int):
+    """The drop-in call with host buffers: nraps_monte_carlo end to end."""
+    from nraps_gb300 import api
+    ctx = api.Context(seed=seed, device=device, **ARMS[arm])
+    small = prob.with_(histories=1000, generations=2, skip=1)
+    ctx.monte_carlo(small)  # context warm-up (module load), untimed
+    t = time.perf_counter()
+    r = ctx.monte_carlo(prob)
+    dt = time.perf_counter() - t
+    ctx.close()
+    inputs = [prob.sigt, prob.sigs, prob.mu, prob.siga, prob.sigf, prob.nut, prob.chit, prob.scat,
+              prob.inv_sigtr, prob.matid, prob.delta_x, prob.mesh_left, prob.mesh_right, prob.fuel_indices]
+    h2d = sum(a.nbytes for a in inputs)
+    d2h = (r.flux.nbytes + r.assembly_average.nbytes + r.fission_source.nbytes + r.k.nbytes + r.k_fund.nbytes
+           + r.k64.nbytes + r.entropy.nbytes + r.flux_mean.nbytes + r.flux_sem.nbytes)
+    g = prob.generations
+    return dict(value=prob.histories * g / dt, seconds=dt, h2d=h2d / g, d2h=d2h / g, k_mean=r.stats.k_mean,
+                k_sigma=r.stats.k_sigma)
+
+
+def cpu_reference_rate(prob, budget_s: float, threads: int):
+    """The reference algorithm on the host cores: COMPAT, f32 arithmetic and
+    f32 tallies, T threads (histories split as src/mc_code.rs:300-307)."""
+    from nraps_gb300 import abi
+    from oracle import oracle as O
+    o = abi.make_opts(seed=12345, mode=abi.MODE_COMPAT, precision=abi.PREC_FP32, compat_threads=threads)
+    n = max(threads * 20, 1000)
+    while True:
+        q = prob.with_(histories=n, generations=2, skip=1)
+        t = time.perf_counter()
+        O.monte_carlo(q, o, threads=threads, acc64=False, max_generations=1)
+        dt = time.perf_counter() - t
+        if dt > 0.5 or n >= prob.histories:
+            break
+        n = min(prob.histories, n * 4)
+    rate = n / dt
+    n_sample = int(min(prob.histories, max(threads * 10, rate * budget_s)))
+    return rate, n_sample
+
+
+def run_reference_arm(args):
+    from nraps_gb300 import abi
+    from oracle import oracle as O
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    prob = make_workload(args.workload, args.seed, args.warmup, args.steps)
+    threads = max(1, (os.cpu_count() or 2) - 1)
+    per_step = max(0.05, min(1.0, args.reference_budget_s / max(1, args.steps + args.warmup)))
+    rate, n = cpu_reference_rate(prob, per_step, threads)
+    o = abi.make_opts(seed=12345, mode=abi.MODE_COMPAT, precision=abi.PREC_FP32, compat_threads=threads)
+    q = prob.with_(histories=n, generations=2, skip=1)
+    for _ in range(args.warmup):
+        O.monte_carlo(q, o, threads=threads, acc64=False, max_generations=1)
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        O.monte_carlo(q, o, threads=threads, acc64=False, max_generations=1)
+    dt = time.perf_counter() - t
+    hist = (n + threads) * args.steps
+    value = hist / dt
+    sample = (f"{args.steps} generations of {n}+{threads} histories of {args.workload} "
+              f"(COMPAT f32, CPU restatement of src/mc_code.rs)")
+    line = {"impl": "reference", "metric": "histories/s", "value": value, "unit": "histories/s",
+            "n_gpus": 0, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * dt / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": {"workload": args.workload, "histories_per_step": n + threads},
+            "cpu_baseline": {"value": value, "unit": "histories/s", "cores": threads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": "histories/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=50)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="single_large")
+    ap.add_argument("--arm", default="auto", choices=["auto", "event", "plain"])
+    ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--plain-steps", type=int, default=5)
+    ap.add_argument("--cpu-budget-s", type=float, default=12.0)
+    ap.add_argument("--reference-budget-s", type=float, default=120.0)
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        raise SystemExit("--warmup must be >= 3")
+    if args.impl == "reference":
+        return run_reference_arm(args)
+
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    from nraps_gb300 import abi, api
+    api.load()
+    seed = args.seed + 1000 * rank  # independent replicas per rank
+    prob = make_workload(args.workload, args.seed, args.warmup, args.steps)
+
+    arm = args.arm
+    if arm == "auto":
+        arm = "event"
+        try:
+            c = api.Context(seed=1, device=local, **ARMS["event"])
+            c.solve(prob.with_(histories=1000, generations=2, skip=1))
+            c.close()
+        except api.NrapsError:
+            arm = "plain"
+    clocks = Clocks(local)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    d = measure_device(prob, arm, args.steps, args.warmup, seed, local)
+    clk = clocks.stop()
+    ms = d["ms"]
+    if world > 1:
+        t = torch.tensor([ms], device=f"cuda:{local}", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+        torch.distributed.barrier()
+    value = world * d["histories"] / (ms / 1000.0)
+
+    # the plain FP64 history-per-thread kernel on the same workload, a few
+    # generations (its throughput is the 10x target's denominator)
+    plain = None
+    if arm == "event" and args.plain_steps > 0:
+        pp = prob.with_(generations=3 + args.plain_steps, skip=3)
+        dp = measure_device(pp, "plain", args.plain_steps, 3, seed, local)
+        plain = {"histories_per_s": dp["histories"] / (dp["ms"] / 1000.0),
+                 "collisions_per_s": dp["collisions"] / (dp["ms"] / 1000.0),
+                 "steps": args.plain_steps, "dtype": "f64"}
+
+    e2e = None
+    if not args.no_e2e:
+        e = measure_e2e(prob, arm, seed, local)
+        e2e = {"value": world * e["value"], "unit": "histories/s", "h2d_bytes_per_step": e["h2d"],
+               "d2h_bytes_per_step": e["d2h"], "seconds": e["seconds"], "call": "nraps_monte_carlo"}
+
+    peak, peak_kind = peaks()
+    per_launch_ms = d["transport_ms"] / max(1, d["transport_launches"])
+    coll_per_launch = d["collisions"] / max(1, d["transport_launches"])
+    achieved = ALG_BYTES_PER_COLLISION * coll_per_launch / (per_launch_ms / 1000.0) / 1e9 if per_launch_ms > 0 else 0.0
+    tpc = traffic_per_collision()
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_kind": peak_kind,
+                "traffic": (tpc * coll_per_launch) if tpc else None,
+                "kernel": "event_transport" if arm == "event" else "plain_transport",
+                "bytes_per_collision": ALG_BYTES_PER_COLLISION,
+                "launches": d["transport_launches"], "avg_launch_ms": per_launch_ms}
+
+    cpu = None
+    if rank == 0:
+        threads = max(1, (os.cpu_count() or 2) - 1)
+        from oracle import oracle as O
+        o = abi.make_opts(seed=12345, mode=abi.MODE_COMPAT, precision=abi.PREC_FP32, compat_threads=threads)
+        rate, n = cpu_reference_rate(prob, args.cpu_budget_s, threads)
+        q = prob.with_(histories=n, generations=2, skip=1)
+        t = time.perf_counter()
+        O.monte_carlo(q, o, threads=threads, acc64=False, max_generations=1)
+        dt = time.perf_counter() - t
+        cpu = {"value": (n + threads) / dt, "unit": "histories/s", "cores": threads, "kind": "port",
+               "sample": f"1 generation of {n}+{threads} histories of {args.workload}, COMPAT f32, "
+                         f"CPU restatement of src/mc_code.rs (reference thread policy)"}
+
+    if rank == 0:
+        line = {
+            "metric": "histories/s", "value": value, "unit": "histories/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32+f64" if arm == "event" else "f64", "data": "synthetic",
+            "config": {"workload": args.workload, "histories_per_step": prob.histories,
+                       "cells": prob.n_cells, "groups": prob.energygroups,
+                       "generations": f"{args.warmup} inactive (warm-up) + {args.steps} active (timed)",
+                       "form": "event Woodcock FP32 flights + FP64 tallies" if arm == "event"
+                       else "plain history-per-thread FP64", "l2": "flushed between steps (256 MB write)",
+                       "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
+            "sigma_k_pcm": d["k_sigma"] * 1e5, "k_mean": d["k_mean"],
+            "collisions_per_s": world * d["collisions"] / (ms / 1000.0),
+            "gpu_launches": d["launches"],
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "plain": plain, "clocks": clk,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

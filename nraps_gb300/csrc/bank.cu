@@ -1,0 +1,242 @@
+/*
+ * bank.cu — fission-bank ordering, Shannon entropy and the per-generation
+ * FP64 finalize (k estimator, flux/fission-source accumulation).
+ *
+ * Bank order.  Transport kernels append sites in whatever order warps reach
+ * them, each tagged (parent history, sequence number within that history),
+ * and every history writes how many sites it banked.  An exclusive scan of
+ * those counts gives each parent's first slot, so site (p, s) lands at
+ * offset[p] + s: the ordered bank is a pure function of the histories, not of
+ * thread scheduling.  The next generation's particle i takes ordered site
+ * floor(i * B / N) (systematic resampling to N source particles).
+ *
+ * Finalize follows the reference's generation bookkeeping
+ * (src/mc_code.rs:340-363) in FP64: flux = tally/(k*N*dx),
+ * fission_source = nu*sigf*flux, conversion = 3565e6*k*36.2 /
+ * (200e6*1.602176634e-19*nu[M]*L); COMPAT takes k_new = sum(k*dx*fs) over the
+ * tally bins, PHYSICS/BANK take the exact fixed-point track-length score.
+ * Reductions use a fixed tree, so repeated runs give identical k.
+ */
+#include "engine.cuh"
+#include "nr_math.h"
+
+namespace {
+
+constexpr int SCAN_THREADS = 1024;
+constexpr int SCAN_ITEMS = 4;
+constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
+
+__device__ __forceinline__ uint32_t warp_incl_scan(uint32_t v) {
+    int lane = threadIdx.x & 31;
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t n = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += n;
+    }
+    return v;
+}
+
+/* block-wide exclusive scan of one value per thread; returns the total */
+__device__ uint32_t block_excl_scan(uint32_t v, uint32_t* excl, uint32_t* smem_warp) {
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    uint32_t inc = warp_incl_scan(v);
+    if (lane == 31) smem_warp[w] = inc;
+    __syncthreads();
+    if (w == 0) {
+        uint32_t t = lane < nw ? smem_warp[lane] : 0u;
+        uint32_t ti = warp_incl_scan(t);
+        if (lane < nw) smem_warp[lane] = ti - t;
+        if (lane == 31) smem_warp[32] = ti;
+    }
+    __syncthreads();
+    *excl = inc - v + smem_warp[w];
+    uint32_t total = smem_warp[32];
+    __syncthreads();
+    return total;
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) scan_tile_sums(const uint32_t* count, uint64_t n,
+                                                               uint32_t* block_sums) {
+    __shared__ uint32_t sw[33];
+    uint64_t base = (uint64_t)blockIdx.x * SCAN_TILE + (uint64_t)threadIdx.x * SCAN_ITEMS;
+    uint32_t s = 0;
+    for (int i = 0; i < SCAN_ITEMS; ++i) if (base + i < n) s += count[base + i];
+    uint32_t ex;
+    uint32_t tot = block_excl_scan(s, &ex, sw);
+    if (threadIdx.x == 0) block_sums[blockIdx.x] = tot;
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) scan_top(uint32_t* block_sums, uint64_t nb, GenState* st) {
+    __shared__ uint32_t sw[33];
+    uint32_t carry = 0;
+    for (uint64_t b0 = 0; b0 < nb; b0 += SCAN_THREADS) {
+        uint64_t i = b0 + threadIdx.x;
+        uint32_t v = i < nb ? block_sums[i] : 0u;
+        uint32_t ex;
+        uint32_t tot = block_excl_scan(v, &ex, sw);
+        if (i < nb) block_sums[i] = carry + ex;
+        carry += tot;
+    }
+    if (threadIdx.x == 0) st->n_bank_next = carry;
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) scan_apply(const uint32_t* count, uint64_t n,
+                                                           const uint32_t* block_sums, uint32_t* offsets) {
+    __shared__ uint32_t sw[33];
+    uint64_t base = (uint64_t)blockIdx.x * SCAN_TILE + (uint64_t)threadIdx.x * SCAN_ITEMS;
+    uint32_t v[SCAN_ITEMS];
+    uint32_t s = 0;
+    for (int i = 0; i < SCAN_ITEMS; ++i) { v[i] = (base + i < n) ? count[base + i] : 0u; s += v[i]; }
+    uint32_t ex;
+    block_excl_scan(s, &ex, sw);
+    uint32_t run = block_sums[blockIdx.x] + ex;
+    for (int i = 0; i < SCAN_ITEMS; ++i) {
+        if (base + i < n) offsets[base + i] = run;
+        run += v[i];
+    }
+}
+
+__global__ void bank_scatter(BankArgs a) {
+    const GenState* st = a.st;
+    uint64_t n = st->n_sites;
+    if (n > a.sink.cap) n = a.sink.cap;
+    nraps_site* out = a.bank[(st->gen + 1) & 1];
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t pos = (uint64_t)a.offsets[a.sink.parent[i]] + a.sink.seq[i];
+        if (pos < a.bank_cap) {
+            nraps_site s;
+            s.x = a.sink.x[i];
+            s.cell = a.sink.cell[i];
+            s.group = a.sink.group[i];
+            s.pad = 0;
+            out[pos] = s;
+            atomicAdd(&a.hist[s.cell], 1u);
+        }
+    }
+}
+
+__device__ __forceinline__ double block_sum_d(double v, double* sm) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if (lane == 0) sm[w] = v;
+    __syncthreads();
+    double r = 0.0;
+    if (threadIdx.x == 0) for (int i = 0; i < nw; ++i) r += sm[i];
+    __syncthreads();
+    return r;
+}
+
+constexpr int FIN_THREADS = 256;
+
+/* one thread per cell: reads and clears the cell's G tally bins */
+__global__ void __launch_bounds__(FIN_THREADS) finalize_bins(FinalizeArgs a) {
+    __shared__ double sm[FIN_THREADS / 32];
+    const GenState* st = a.st;
+    const uint64_t gen = st->gen;
+    const double k = st->k;
+    const bool active = gen >= a.skip;
+    double fund;
+    if (a.mode == NRAPS_MODE_COMPAT) fund = 1.0 / (double)(uint64_t)(a.generations - (a.skip - 1));
+    else fund = 1.0 / (double)(a.generations - a.skip);
+    const double conversion = a.conv_const * k;
+    const double N = (double)a.N;
+    double kpart = 0.0, hpart = 0.0;
+    const double B = (double)st->n_bank_next;
+    for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < a.nc;
+         c += (uint64_t)gridDim.x * blockDim.x) {
+        double dx = a.dx64[c];
+        uint32_t m = a.mat[c];
+        double fs = 0.0;
+        for (uint32_t g = 0; g < a.G; ++g) {
+            uint64_t bin = (uint64_t)g * a.nc + c;
+            double t = a.tally[bin];
+            a.tally[bin] = 0.0;
+            double flux = t / (k * N * dx);
+            double f = a.nsf64[m + (uint64_t)a.M * g] * flux;
+            kpart += k * dx * f;
+            fs += f;
+            double phi = t / (N * dx);
+            if (active) {
+                a.flux_acc[bin] += flux * conversion * fund;
+                a.flux_sum[bin] += phi;
+                a.flux_sq[bin] += phi * phi;
+            }
+        }
+        if (active) a.fs_acc[c] += fs * fund;
+        if (a.bank_mode) {
+            uint32_t cnt = a.hist[c];
+            a.hist_w[c] = 0;
+            if (cnt && B > 0.0) {
+                double p = (double)cnt / B;
+                hpart -= p * nr_log(p) * 1.4426950408889634;   /* log2 */
+            }
+        }
+    }
+    double ks = block_sum_d(kpart, sm);
+    double hs = block_sum_d(hpart, sm);
+    if (threadIdx.x == 0) {
+        a.partials[2 * blockIdx.x] = ks;
+        a.partials[2 * blockIdx.x + 1] = hs;
+    }
+}
+
+__global__ void finalize_state(FinalizeArgs a) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    GenState* st = a.st;
+    double ks = 0.0, hs = 0.0;
+    for (uint32_t b = 0; b < a.n_blocks; ++b) { ks += a.partials[2 * b]; hs += a.partials[2 * b + 1]; }
+    double k_new = (a.mode == NRAPS_MODE_COMPAT) ? ks : nr_unfix(st->kq) / (double)a.N;
+    uint64_t gen = st->gen;
+    if (gen < a.generations) {
+        a.k64[gen] = k_new;
+        a.entropy[gen] = a.bank_mode ? hs : 0.0;
+    }
+    if (a.bank_mode) {
+        unsigned long long b = st->n_bank_next;
+        if (b > a.bank_cap) { b = a.bank_cap; st->error |= NR_ERR_CAPACITY; }
+        st->n_bank = b;
+        if (b == 0) st->error |= NR_ERR_EMPTY;
+        st->tot_sites += st->n_sites;
+    }
+    st->tot_collisions += st->collisions;
+    st->tot_virtual += st->virtual_collisions;
+    st->tot_crossings += st->crossings;
+    st->tot_absorbed += st->absorbed;
+    st->tot_leaked += st->leaked;
+    st->tot_capped += st->capped;
+    st->collisions = st->virtual_collisions = st->crossings = 0;
+    st->absorbed = st->leaked = st->capped = 0;
+    st->n_sites = 0;
+    st->n_bank_next = 0;
+    st->kq = 0;
+    st->k = k_new;
+    st->gen = gen + 1;
+}
+
+}  // namespace
+
+int launch_bank_order(const BankArgs& a, cudaStream_t s) {
+    uint64_t nb = (a.n_hist + SCAN_TILE - 1) / SCAN_TILE;
+    if (nb == 0) return 0;
+    scan_tile_sums<<<(unsigned)nb, SCAN_THREADS, 0, s>>>(a.sink.count, a.n_hist, a.block_sums);
+    scan_top<<<1, SCAN_THREADS, 0, s>>>(a.block_sums, nb, a.st);
+    scan_apply<<<(unsigned)nb, SCAN_THREADS, 0, s>>>(a.sink.count, a.n_hist, a.block_sums, a.offsets);
+    uint64_t grid = (a.sink.cap + 255) / 256;
+    if (grid > 152 * 16) grid = 152 * 16;
+    if (grid == 0) grid = 1;
+    bank_scatter<<<(unsigned)grid, 256, 0, s>>>(a);
+    return cudaPeekAtLastError() == cudaSuccess ? 4 : -1;
+}
+
+int launch_finalize(const FinalizeArgs& a, cudaStream_t s) {
+    finalize_bins<<<a.n_blocks, FIN_THREADS, 0, s>>>(a);
+    finalize_state<<<1, 32, 0, s>>>(a);
+    return cudaPeekAtLastError() == cudaSuccess ? 2 : -1;
+}
+
+uint32_t finalize_blocks_for(uint64_t nc) {
+    uint64_t b = (nc + FIN_THREADS - 1) / FIN_THREADS;
+    if (b > 152 * 4) b = 152 * 4;
+    if (b == 0) b = 1;
+    return (uint32_t)b;
+}

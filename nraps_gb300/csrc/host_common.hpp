@@ -1,0 +1,11 @@
+/* host_common.hpp — error text shared by the host-side entry points. */
+#ifndef NRAPS_HOST_COMMON_HPP
+#define NRAPS_HOST_COMMON_HPP
+#include <string>
+
+namespace nraps_host {
+/* Message of the last failure of a call made without a context, per thread. */
+void set_error(const std::string& msg);
+const char* last_error();
+}  // namespace nraps_host
+#endif

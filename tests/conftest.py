@@ -1,0 +1,37 @@
+import os
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
+
+
+@pytest.fixture(scope="session")
+def lib():
+    from nraps_gb300 import api
+    from nraps_gb300.build import build
+    build()
+    return api.load()
+
+
+@pytest.fixture(scope="session")
+def ctx_factory(lib):
+    from nraps_gb300 import api
+    made = []
+
+    def make(**kw):
+        c = api.Context(**kw)
+        made.append(c)
+        return c
+
+    yield make
+    for c in made:
+        c.close()
