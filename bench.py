@@ -254,6 +254,7 @@ def main():
     ap.add_argument("--cpu-budget-s", type=float, default=12.0)
     ap.add_argument("--reference-budget-s", type=float, default=120.0)
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
     args = ap.parse_args()
     if args.warmup < 3:
         raise SystemExit("--warmup must be >= 3")
@@ -325,7 +326,7 @@ def main():
                 "launches": d["transport_launches"], "avg_launch_ms": per_launch_ms}
 
     cpu = None
-    if rank == 0:
+    if rank == 0 and not args.no_cpu:
         threads = max(1, (os.cpu_count() or 2) - 1)
         from oracle import oracle as O
         o = abi.make_opts(seed=12345, mode=abi.MODE_COMPAT, precision=abi.PREC_FP32, compat_threads=threads)

@@ -86,7 +86,10 @@ typedef struct nraps_opts {
     uint32_t use_graphs;         /* 1 = replay each generation as a CUDA graph */
     double   bank_factor;        /* bank capacity = bank_factor*N (+slack); 0=3 */
     uint32_t entropy_bins;       /* Shannon-entropy bins: must be 0 (one per cell) */
-    uint32_t reserved[7];
+    uint32_t exact_log;          /* WOODCOCK: 1 = flights use the shared software
+                                    logarithm (bit-reproducible on a CPU);
+                                    0 = the hardware log2 unit (fast)         */
+    uint32_t reserved[6];
 } nraps_opts;
 
 /* Fill *o with the defaults (FP64 surface tracking, COMPAT, seed 1). */

@@ -19,40 +19,15 @@
  */
 #include "engine.cuh"
 #include "nr_math.h"
+#include "dev_util.cuh"
+
+using nrdev::block_excl_scan;
 
 namespace {
 
 constexpr int SCAN_THREADS = 1024;
 constexpr int SCAN_ITEMS = 4;
 constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
-
-__device__ __forceinline__ uint32_t warp_incl_scan(uint32_t v) {
-    int lane = threadIdx.x & 31;
-    for (int o = 1; o < 32; o <<= 1) {
-        uint32_t n = __shfl_up_sync(0xffffffffu, v, o);
-        if (lane >= o) v += n;
-    }
-    return v;
-}
-
-/* block-wide exclusive scan of one value per thread; returns the total */
-__device__ uint32_t block_excl_scan(uint32_t v, uint32_t* excl, uint32_t* smem_warp) {
-    int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    uint32_t inc = warp_incl_scan(v);
-    if (lane == 31) smem_warp[w] = inc;
-    __syncthreads();
-    if (w == 0) {
-        uint32_t t = lane < nw ? smem_warp[lane] : 0u;
-        uint32_t ti = warp_incl_scan(t);
-        if (lane < nw) smem_warp[lane] = ti - t;
-        if (lane == 31) smem_warp[32] = ti;
-    }
-    __syncthreads();
-    *excl = inc - v + smem_warp[w];
-    uint32_t total = smem_warp[32];
-    __syncthreads();
-    return total;
-}
 
 __global__ void __launch_bounds__(SCAN_THREADS) scan_tile_sums(const uint32_t* count, uint64_t n,
                                                                uint32_t* block_sums) {
@@ -65,7 +40,8 @@ __global__ void __launch_bounds__(SCAN_THREADS) scan_tile_sums(const uint32_t* c
     if (threadIdx.x == 0) block_sums[blockIdx.x] = tot;
 }
 
-__global__ void __launch_bounds__(SCAN_THREADS) scan_top(uint32_t* block_sums, uint64_t nb, GenState* st) {
+__global__ void __launch_bounds__(SCAN_THREADS) scan_top(uint32_t* block_sums, uint64_t nb,
+                                                         unsigned long long* total, uint32_t* offsets_end) {
     __shared__ uint32_t sw[33];
     uint32_t carry = 0;
     for (uint64_t b0 = 0; b0 < nb; b0 += SCAN_THREADS) {
@@ -76,7 +52,10 @@ __global__ void __launch_bounds__(SCAN_THREADS) scan_top(uint32_t* block_sums, u
         if (i < nb) block_sums[i] = carry + ex;
         carry += tot;
     }
-    if (threadIdx.x == 0) st->n_bank_next = carry;
+    if (threadIdx.x == 0) {
+        if (total) *total = carry;
+        if (offsets_end) *offsets_end = carry;
+    }
 }
 
 __global__ void __launch_bounds__(SCAN_THREADS) scan_apply(const uint32_t* count, uint64_t n,
@@ -210,17 +189,25 @@ __global__ void finalize_state(FinalizeArgs a) {
     st->n_bank_next = 0;
     st->kq = 0;
     st->k = k_new;
+    st->inv_kf = (float)(1.0 / k_new);
     st->gen = gen + 1;
 }
 
 }  // namespace
 
-int launch_bank_order(const BankArgs& a, cudaStream_t s) {
-    uint64_t nb = (a.n_hist + SCAN_TILE - 1) / SCAN_TILE;
+int launch_exclusive_scan(const uint32_t* count, uint64_t n, uint32_t* block_sums, uint32_t* offsets,
+                          unsigned long long* total, cudaStream_t s) {
+    uint64_t nb = (n + SCAN_TILE - 1) / SCAN_TILE;
     if (nb == 0) return 0;
-    scan_tile_sums<<<(unsigned)nb, SCAN_THREADS, 0, s>>>(a.sink.count, a.n_hist, a.block_sums);
-    scan_top<<<1, SCAN_THREADS, 0, s>>>(a.block_sums, nb, a.st);
-    scan_apply<<<(unsigned)nb, SCAN_THREADS, 0, s>>>(a.sink.count, a.n_hist, a.block_sums, a.offsets);
+    scan_tile_sums<<<(unsigned)nb, SCAN_THREADS, 0, s>>>(count, n, block_sums);
+    scan_top<<<1, SCAN_THREADS, 0, s>>>(block_sums, nb, total, offsets + n);
+    scan_apply<<<(unsigned)nb, SCAN_THREADS, 0, s>>>(count, n, block_sums, offsets);
+    return cudaPeekAtLastError() == cudaSuccess ? 3 : -1;
+}
+
+int launch_bank_order(const BankArgs& a, cudaStream_t s) {
+    if (launch_exclusive_scan(a.sink.count, a.n_hist, a.block_sums, a.offsets, &a.st->n_bank_next, s) < 0)
+        return -1;
     uint64_t grid = (a.sink.cap + 255) / 256;
     if (grid > 152 * 16) grid = 152 * 16;
     if (grid == 0) grid = 1;

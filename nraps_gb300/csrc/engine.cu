@@ -180,19 +180,25 @@ int create_session(nraps_ctx* ctx, const nraps_problem* p, bool with_records, nr
     uint32_t nfb = finalize_blocks_for(s->nc);
     CK(s->partials.alloc(2 * (size_t)nfb * 8));
     bool bank = s->o.mode == NRAPS_MODE_BANK;
+    bool woodcock = s->o.tracking == NRAPS_TRACK_WOODCOCK;
     double bf = s->o.bank_factor > 0 ? s->o.bank_factor : 3.0;
     s->cap = bank ? (uint64_t)(bf * (double)s->N) + 1024 : 0;
     if (bank) {
-        CK(s->sx.alloc(s->cap * 4)); CK(s->scell.alloc(s->cap * 4)); CK(s->sgroup.alloc(s->cap * 4));
-        CK(s->sparent.alloc(s->cap * 4)); CK(s->sseq.alloc(s->cap * 4));
-        CK(s->scount.alloc(s->n_hist * 4)); CK(s->offsets.alloc(s->n_hist * 4));
-        CK(s->block_sums.alloc(((s->n_hist + 4095) / 4096 + 1) * 4));
+        if (!woodcock) {   /* the event engine keeps its own site slabs */
+            CK(s->sx.alloc(s->cap * 4)); CK(s->scell.alloc(s->cap * 4)); CK(s->sgroup.alloc(s->cap * 4));
+            CK(s->sparent.alloc(s->cap * 4)); CK(s->sseq.alloc(s->cap * 4));
+            CK(s->scount.alloc(s->n_hist * 4)); CK(s->offsets.alloc((s->n_hist + 1) * 4));
+            CK(s->block_sums.alloc(((s->n_hist + 4095) / 4096 + 1) * 4));
+            CK(cudaMemsetAsync(s->scount.p, 0, s->n_hist * 4, sm));
+        }
         CK(s->bank0.alloc(s->cap * sizeof(nraps_site))); CK(s->bank1.alloc(s->cap * sizeof(nraps_site)));
         CK(s->hist.alloc(s->nc * 4));
         CK(cudaMemsetAsync(s->hist.p, 0, s->nc * 4, sm));
-        CK(cudaMemsetAsync(s->scount.p, 0, s->n_hist * 4, sm));
     }
-    if (with_records) CK(s->records.alloc(s->n_hist * sizeof(nraps_history_record)));
+    if (with_records) {
+        CK(s->records.alloc(s->n_hist * sizeof(nraps_history_record)));
+        CK(cudaMemsetAsync(s->records.p, 0, s->n_hist * sizeof(nraps_history_record), sm));
+    }
     CK(cudaMemsetAsync(s->tally.p, 0, nb * 8, sm));
     CK(cudaMemsetAsync(s->flux_acc.p, 0, nb * 8, sm));
     CK(cudaMemsetAsync(s->flux_sum.p, 0, nb * 8, sm));
@@ -203,6 +209,7 @@ int create_session(nraps_ctx* ctx, const nraps_problem* p, bool with_records, nr
     GenState g0;
     std::memset(&g0, 0, sizeof g0);
     g0.k = (double)p->k_new;
+    g0.inv_kf = (float)(1.0 / g0.k);
     CK(cudaMemcpyAsync(s->state.p, &g0, sizeof g0, cudaMemcpyHostToDevice, sm));
 
     s->ba.st = s->state.as<GenState>();
@@ -241,11 +248,22 @@ int create_session(nraps_ctx* ctx, const nraps_problem* p, bool with_records, nr
     f.partials = s->partials.as<double>(); f.n_blocks = nfb;
     f.bank_mode = bank ? 1 : 0;
     f.bank_cap = s->cap;
-    if (s->o.tracking == NRAPS_TRACK_WOODCOCK) {
+    if (woodcock) {
         s->ev.reset(new EventEngine());
         std::string e2;
-        int est = s->ev->init(*p, s->o, s->state.as<GenState>(), s->tally.as<double>(), s->ba.sink,
-                              s->ba.bank[0], s->ba.bank[1], sm, e2);
+        int est = s->ev->configure(s->o, e2);
+        if (est) return set_err(ctx, est, e2);
+        EvBuffers eb;
+        eb.st = s->state.as<GenState>(); eb.tally = s->tally.as<double>();
+        eb.flux_acc = s->flux_acc.as<double>(); eb.fs_acc = s->fs_acc.as<double>();
+        eb.flux_sum = s->flux_sum.as<double>(); eb.flux_sq = s->flux_sq.as<double>();
+        eb.k64 = s->k64.as<double>(); eb.entropy = s->entropy.as<double>();
+        eb.bank[0] = s->bank0.as<nraps_site>(); eb.bank[1] = s->bank1.as<nraps_site>();
+        eb.bank_cap = s->cap; eb.hist = s->hist.as<uint32_t>();
+        eb.generations = s->gens; eb.skip = s->v.skip; eb.seed = s->o.seed;
+        if (s->ev->add_instance(*p, eb, e2) < 0) return set_err(ctx, NRAPS_ERR_INVALID, e2);
+        if (with_records) s->ev->set_records(s->records.as<nraps_history_record>());
+        est = s->ev->commit(sm, e2);
         if (est) return set_err(ctx, est, e2);
     }
     s->cell_dx_host.assign(p->mesh.delta_x, p->mesh.delta_x + s->nc);
@@ -254,16 +272,16 @@ int create_session(nraps_ctx* ctx, const nraps_problem* p, bool with_records, nr
     return NRAPS_OK;
 }
 
-/* Enqueue the transport phase of one generation; returns kernels launched. */
+/* Enqueue the transport phase of one (plain) generation; returns kernels launched. */
 int enqueue_transport(nraps_session* s, cudaStream_t sm) {
     int block = (int)s->o.block_size;
-    if (s->ev) return s->ev->enqueue_generation(sm);
     if (s->o.precision == NRAPS_PREC_FP32) return launch_plain<float>(s->pf, s->o.mode, block, sm);
     return launch_plain<double>(s->pd, s->o.mode, block, sm);
 }
 
 /* Whole generation: transport, bank ordering, finalize. */
 int enqueue_generation(nraps_session* s, cudaStream_t sm, cudaEvent_t t0, cudaEvent_t t1) {
+    if (s->ev) return s->ev->enqueue_generation(sm, true, t0, t1);
     int n = 0, r;
     if (t0) cudaEventRecord(t0, sm);
     r = enqueue_transport(s, sm);
@@ -573,8 +591,6 @@ int nraps_trace_generation(nraps_ctx* ctx, const nraps_problem* problem, uint64_
                            nraps_site* sites_out, uint64_t cap_sites_out, uint64_t* n_sites_out,
                            uint64_t* k_fixed_out) {
     if (!ctx || !problem || !records) return set_err(ctx, NRAPS_ERR_INVALID, "NULL argument");
-    if (ctx->opts.tracking != NRAPS_TRACK_SURFACE)
-        return set_err(ctx, NRAPS_ERR_INVALID, "per-history traces come from the SURFACE (plain) kernel");
     cudaSetDevice(ctx->device);
     nraps_problem p = *problem;
     if (p.variables.generations <= generation) p.variables.generations = generation + 1;
@@ -587,7 +603,7 @@ int nraps_trace_generation(nraps_ctx* ctx, const nraps_problem* problem, uint64_
     cudaStream_t sm = ctx->stream;
     GenState g0;
     std::memset(&g0, 0, sizeof g0);
-    g0.gen = generation; g0.k = k;
+    g0.gen = generation; g0.k = k; g0.inv_kf = (float)(1.0 / k);
     if (sites_in && n_sites_in) {
         if (s->o.mode != NRAPS_MODE_BANK) return set_err(ctx, NRAPS_ERR_INVALID, "sites_in needs BANK mode");
         if (n_sites_in > s->cap) return set_err(ctx, NRAPS_ERR_CAPACITY, "sites_in exceeds the bank capacity");
@@ -596,13 +612,19 @@ int nraps_trace_generation(nraps_ctx* ctx, const nraps_problem* problem, uint64_
         g0.n_bank = n_sites_in;
     }
     CK(cudaMemcpyAsync(s->state.p, &g0, sizeof g0, cudaMemcpyHostToDevice, sm));
-    int r = enqueue_transport(s, sm);
-    if (r < 0) return set_err(ctx, NRAPS_ERR_CUDA, std::string("kernel launch failed: ") + cudaGetErrorString(cudaGetLastError()));
-    ctx->launches += (uint64_t)r;
-    if (s->o.mode == NRAPS_MODE_BANK) {
-        r = launch_bank_order(s->ba, sm);
-        if (r < 0) return set_err(ctx, NRAPS_ERR_CUDA, "bank ordering launch failed");
+    if (s->ev) {
+        int r = s->ev->enqueue_generation(sm, false);
+        if (r < 0) return set_err(ctx, NRAPS_ERR_CUDA, std::string("kernel launch failed: ") + cudaGetErrorString(cudaGetLastError()));
         ctx->launches += (uint64_t)r;
+    } else {
+        int r = enqueue_transport(s, sm);
+        if (r < 0) return set_err(ctx, NRAPS_ERR_CUDA, std::string("kernel launch failed: ") + cudaGetErrorString(cudaGetLastError()));
+        ctx->launches += (uint64_t)r;
+        if (s->o.mode == NRAPS_MODE_BANK) {
+            r = launch_bank_order(s->ba, sm);
+            if (r < 0) return set_err(ctx, NRAPS_ERR_CUDA, "bank ordering launch failed");
+            ctx->launches += (uint64_t)r;
+        }
     }
     CK(cudaStreamSynchronize(sm));
     CK(cudaMemcpy(records, s->records.p, s->n_hist * sizeof(nraps_history_record), cudaMemcpyDeviceToHost));
@@ -610,7 +632,16 @@ int nraps_trace_generation(nraps_ctx* ctx, const nraps_problem* problem, uint64_
     GenState g;
     CK(cudaMemcpy(&g, s->state.p, sizeof g, cudaMemcpyDeviceToHost));
     if (k_fixed_out) *k_fixed_out = g.kq;
-    uint64_t B = s->o.mode == NRAPS_MODE_BANK ? std::min<uint64_t>(g.n_bank_next, s->cap) : 0;
+    uint64_t B = 0;
+    if (s->o.mode == NRAPS_MODE_BANK) {
+        if (s->ev) {
+            uint32_t tot = 0;
+            CK(cudaMemcpy(&tot, s->ev->offsets() + s->ev->n_total(), 4, cudaMemcpyDeviceToHost));
+            B = std::min<uint64_t>(tot, s->cap);
+        } else {
+            B = std::min<uint64_t>(g.n_bank_next, s->cap);
+        }
+    }
     if (n_sites_out) *n_sites_out = B;
     if (sites_out && B) {
         void* src = ((generation + 1) & 1) ? s->bank1.p : s->bank0.p;

@@ -34,7 +34,8 @@ struct GenState {
     unsigned long long n_bank;  /* ordered sites available as source        */
     unsigned long long n_bank_next;
     unsigned int error;
-    unsigned int pad;
+    float inv_kf;             /* (float)(1/k), read by the FP32 event kernels */
+    double h_acc;             /* entropy accumulator of the event finalize    */
     /* per-generation counters (zeroed by finalize) */
     unsigned long long collisions, virtual_collisions, crossings, absorbed, leaked, capped;
     /* run totals */
@@ -112,6 +113,9 @@ struct FinalizeArgs {
 template <class T>
 int launch_plain(const PlainArgs<T>& a, int mode, int block, cudaStream_t s);
 int launch_bank_order(const BankArgs& a, cudaStream_t s);
+/* offsets[i] = sum(count[0..i)), offsets[n] = total (offsets has n+1 slots) */
+int launch_exclusive_scan(const uint32_t* count, uint64_t n, uint32_t* block_sums, uint32_t* offsets,
+                          unsigned long long* total, cudaStream_t s);
 int launch_finalize(const FinalizeArgs& a, cudaStream_t s);
 int launch_pcg_stream(uint64_t seed, const uint64_t* streams, uint64_t n, uint32_t per,
                       uint32_t* out, cudaStream_t s);

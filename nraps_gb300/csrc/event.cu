@@ -1,11 +1,806 @@
+/*
+ * event.cu — event-based Woodcock transport (FP32 flights, FP64 tallies).
+ *
+ * Particle record in the HBM queues (structure of arrays, 24 bytes):
+ *   x f32 | mu f32 | PCG32 state u64 | particle id u32 | g:4 inst:12 seq:16
+ * Delta tracking: each flight samples d = -ln(u)/maj[g] with the per-group
+ * majorant over the instance's materials; the flight is real with probability
+ * sigtr(x)/maj[g], else virtual.  Real collisions score the collision
+ * estimators (flux 1/sigtr into the tally cell, k score nu*sigf/sigtr in
+ * 2^-32 fixed point), bank floor(nu*sigf/sigtr/k + u) sites (BANK mode),
+ * then absorb with probability siga/sigtr or scatter (transport-corrected
+ * CDF, isotropic mu).  Outer boundaries: vacuum leaks, reflective mirrors.
+ *
+ * Single-instance launches stage the instance's tables (cross sections,
+ * CDFs, majorants, region bounds, materials and lookup grid) in shared
+ * memory; batched launches read each particle's instance tables through L1.
+ * Survivors are compacted per block (one atomic per block per grid-stride
+ * step); fission sites go to one of 128 slabs (one atomic per group of
+ * converged lanes, spread over 128 counters).
+ */
+#include <algorithm>
+#include <cstring>
+
+#include "dev_util.cuh"
 #include "event.cuh"
-struct EventEngine::Impl {};
-EventEngine::EventEngine() : impl_(nullptr) {}
-EventEngine::~EventEngine() {}
-int EventEngine::init(const nraps_problem&, const nraps_opts&, GenState*, double*, SiteSink, nraps_site*,
-                      nraps_site*, cudaStream_t, std::string& err) {
-    err = "WOODCOCK tracking is not available in this build";
-    return NRAPS_ERR_INVALID;
+#include "nr_math.h"
+#include "tables.hpp"
+
+namespace {
+
+constexpr uint32_t NSLAB = 128;
+constexpr uint32_t MAX_PASSES = 16;
+
+struct EvInst {
+    const float* xs;        /* [(m*G+g)*4]: sigtr, pabs, nsf_st, inv_st        */
+    const float* scdf;      /* [(m*G+g)*G + e]                                 */
+    const float* chicdf;    /* [m*G + g]                                       */
+    const float* maj;       /* [g] majorant, [G+g] inverse                     */
+    const float* rleft;     /* R+1                                             */
+    const float* rinvdx;    /* R                                               */
+    const uint8_t* rmat;    /* R                                               */
+    const uint32_t* rfirst; /* R                                               */
+    const uint32_t* rncell; /* R                                               */
+    const uint16_t* grid;   /* nbins                                           */
+    const uint32_t* fuel;   /* nfuel                                           */
+    const float* cleft;     /* nc                                              */
+    const float* cdx;       /* nc                                              */
+    const uint8_t* cmat;    /* nc                                              */
+    const double* nsf64;    /* [m + M*g]                                       */
+    const double* dx64;     /* nc                                              */
+    uint32_t M, G, R, nc, nbins, nfuel;
+    float L, inv_binw, boundl, boundr;
+    uint64_t hist_begin, N, seed;
+    GenState* st;
+    double* tally;
+    double *flux_acc, *fs_acc, *flux_sum, *flux_sq, *k64, *entropy;
+    nraps_site* bank[2];
+    uint64_t bank_cap;
+    uint32_t* hist;
+    uint64_t generations, skip, cell_begin;
+    double conv_const;
+};
+
+struct EvArgs {
+    const EvInst* inst;
+    uint32_t n_inst;
+    const uint64_t* inst_begin;   /* n_inst+1 particle-id prefix              */
+    const uint64_t* cell_begin;   /* n_inst+1 global-cell prefix              */
+    uint64_t n_total, n_cells_total;
+    float* qx[2];
+    float* qmu[2];
+    unsigned long long* qrng[2];
+    uint32_t* qid[2];
+    uint32_t* qpk[2];
+    unsigned long long* qcount;   /* MAX_PASSES+2                             */
+    float* sx;
+    uint32_t* scell;
+    uint32_t* sgi;                /* group | inst << 4                        */
+    uint32_t* sparent;
+    uint32_t* sseq;
+    unsigned long long* slab_count;
+    uint64_t slab_cap;
+    uint32_t* count;
+    uint32_t* offsets;            /* n_total+1                                */
+    GenState* stats;
+    uint64_t max_events;
+    nraps_history_record* rec;
+    int bank;
+};
+
+/* table view: shared memory (single instance) or the instance's globals */
+struct TView {
+    const float* xs;
+    const float* scdf;
+    const float* chi;
+    const float* maj;
+    const float* left;
+    const uint16_t* grid;
+    const uint8_t* rmat;
+    const float* invdx;
+    const uint32_t* first;
+    const uint32_t* ncell;
+    uint32_t G, R, nbins;
+    float L, inv_binw, boundl, boundr;
+};
+
+__device__ __forceinline__ float u24(uint32_t u) { return __fmul_rn(__uint2float_rn(u >> 8), 0x1p-24f); }
+__device__ __forceinline__ float u24pos(uint32_t u) { return __fmul_rn(__uint2float_rn((u >> 8) + 1u), 0x1p-24f); }
+
+template <bool EXACT> __device__ __forceinline__ float neg_log(float u) {
+    if (EXACT) return -nr_logf(u);
+    return -__logf(u);
 }
-int EventEngine::enqueue_generation(cudaStream_t) { return -1; }
-uint64_t EventEngine::launches_per_generation() const { return 0; }
+
+__device__ __forceinline__ uint32_t region_of(const TView& t, float x) {
+    int b = (int)__fmul_rn(x, t.inv_binw);
+    b = b < 0 ? 0 : (b >= (int)t.nbins ? (int)t.nbins - 1 : b);
+    uint32_t r = t.grid[b];
+    while (r + 1 < t.R && x >= t.left[r + 1]) ++r;
+    while (r > 0 && x < t.left[r]) --r;
+    return r;
+}
+
+/* partition_point(cdf[e] < v), clamped to G-1 (chi sampling, as energy()) */
+__device__ __forceinline__ uint32_t chi_group(const float* cdf, uint32_t G, float v) {
+    uint32_t base = 0, size = G;
+    while (size > 1) {
+        uint32_t half = size / 2, mid = base + half;
+        if (cdf[mid] < v) base = mid;
+        size -= half;
+    }
+    uint32_t r = base + ((cdf[base] < v) ? 1u : 0u);
+    return r < G - 1 ? r : G - 1;
+}
+
+struct Part {
+    float x, mu;
+    nr_pcg32 rng;
+    uint32_t id, local, g, inst, seq;
+};
+
+struct Acc {
+    unsigned long long kq;
+    uint32_t coll, virt, absorbed, leaked, capped;
+};
+
+/* Run one particle for up to K real collisions.  Returns true if alive. */
+template <bool EXACT, bool BANK, bool REC>
+__device__ bool run_particle(const EvArgs& a, const EvInst& I, const TView& t, Part& p, uint32_t K,
+                             float inv_k, Acc& acc, unsigned long long& kq_part) {
+    const uint32_t G = t.G;
+    uint64_t events = 0;
+    uint32_t draws = 0;
+    auto next = [&]() -> uint32_t { if (REC) ++draws; return nr_pcg32_next(&p.rng); };
+    nraps_history_record* rec = (REC && p.inst == 0) ? &a.rec[p.local] : nullptr;
+    int fate = -1;
+    for (uint32_t c = 0; c < K && fate < 0; ++c) {
+        uint32_t r = 0, m = 0;
+        /* flight to the next real collision */
+        for (;;) {
+            if (++events > a.max_events) { fate = NRAPS_FATE_CAPPED; break; }
+            float d = __fmul_rn(neg_log<EXACT>(u24pos(next())), t.maj[G + p.g]);
+            p.x = __fadd_rn(p.x, __fmul_rn(p.mu, d));
+            int bounce = 0;
+            while (!(p.x >= 0.0f && p.x <= t.L)) {
+                if (p.x > t.L) {
+                    if (t.boundr > 0.0f) { p.x = __fsub_rn(t.L, __fsub_rn(p.x, t.L)); p.mu = -p.mu; }
+                    else { fate = NRAPS_FATE_LEAKED; break; }
+                } else {
+                    if (t.boundl > 0.0f) { p.x = -p.x; p.mu = -p.mu; }
+                    else { fate = NRAPS_FATE_LEAKED; break; }
+                }
+                if (++bounce > 1000) { fate = NRAPS_FATE_CAPPED; break; }
+            }
+            if (fate >= 0) break;
+            r = region_of(t, p.x);
+            m = t.rmat[r];
+            float s = t.xs[(m * G + p.g) * 4];
+            if (__fmul_rn(u24(next()), t.maj[p.g]) < s) break;
+            acc.virt++;
+            if (REC && rec) rec->crossings++;
+        }
+        if (fate >= 0) break;
+        /* real collision */
+        acc.coll++;
+        const float* X = &t.xs[(m * G + p.g) * 4];
+        float rel = __fmul_rn(__fsub_rn(p.x, t.left[r]), t.invdx[r]);
+        uint32_t nr = t.ncell[r];
+        uint32_t k = rel > 0.0f ? (uint32_t)rel : 0u;
+        if (k >= nr) k = nr - 1;
+        uint32_t cell = t.first[r] + k;
+        float inv_st = X[3], nsf_st = X[2];
+        atomicAdd(&I.tally[(uint64_t)p.g * I.nc + cell], (double)inv_st);
+        unsigned long long q = nr_fix((double)nsf_st);
+        acc.kq += q;
+        kq_part += q;
+        if (REC && rec) {
+            rec->collisions++; rec->track += (double)inv_st; rec->nsf_track += (double)nsf_st;
+            rec->final_cell = cell;
+        }
+        if (BANK) {
+            float nu = __fadd_rn(__fmul_rn(nsf_st, inv_k), u24(next()));
+            int n = (int)floorf(nu);
+            if (n > 64) n = 64;
+            for (int i = 0; i < n; ++i) {
+                uint32_t sg = chi_group(t.chi + m * G, G, u24(next()));
+                uint32_t slab = blockIdx.x % NSLAB;
+                unsigned long long j = nrdev::agg_inc(&a.slab_count[slab]);
+                if (j < a.slab_cap && p.seq < 0xFFFFu) {
+                    uint64_t at = (uint64_t)slab * a.slab_cap + j;
+                    a.sx[at] = p.x;
+                    a.scell[at] = cell;
+                    a.sgi[at] = sg | (p.inst << 4);
+                    a.sparent[at] = p.id;
+                    a.sseq[at] = p.seq;
+                } else {
+                    atomicOr(&I.st->error, NR_ERR_CAPACITY);
+                }
+                p.seq++;
+            }
+        }
+        if (u24(next()) < X[1]) { fate = NRAPS_FATE_ABSORBED; break; }
+        float xi = u24(next());
+        const float* cdf = t.scdf + (m * G + p.g) * G;
+        uint32_t ng = G - 1;
+        for (uint32_t e = 0; e + 1 < G; ++e) if (xi < cdf[e]) { ng = e; break; }
+        p.g = ng;
+        p.mu = __fsub_rn(__fmul_rn(2.0f, u24(next())), 1.0f);
+    }
+    if (REC && rec) rec->draws += draws;
+    if (fate < 0) return true;
+    if (fate == NRAPS_FATE_ABSORBED) acc.absorbed++;
+    else if (fate == NRAPS_FATE_LEAKED) acc.leaked++;
+    else { acc.capped++; atomicOr(&I.st->error, NR_ERR_CAPPED); }
+    if (BANK) a.count[p.id] = p.seq;
+    if (REC && rec) {
+        rec->fate = fate; rec->final_group = p.g; rec->final_x = (double)p.x;
+        rec->n_sites = p.seq;
+    }
+    return false;
+}
+
+__device__ __forceinline__ TView global_view(const EvInst& I) {
+    TView t;
+    t.xs = I.xs; t.scdf = I.scdf; t.chi = I.chicdf; t.maj = I.maj; t.left = I.rleft;
+    t.grid = I.grid; t.rmat = I.rmat; t.invdx = I.rinvdx; t.first = I.rfirst; t.ncell = I.rncell;
+    t.G = I.G; t.R = I.R; t.nbins = I.nbins; t.L = I.L; t.inv_binw = I.inv_binw;
+    t.boundl = I.boundl; t.boundr = I.boundr;
+    return t;
+}
+
+/* shared-memory footprint of one instance's tables */
+__host__ __device__ __forceinline__ size_t smem_words(uint32_t M, uint32_t G, uint32_t R, uint32_t nbins) {
+    size_t f = (size_t)M * G * 4 + (size_t)M * G * G + (size_t)M * G + 2 * G + (R + 1) + 3 * (size_t)R;
+    size_t bytes = f * 4 + (size_t)nbins * 2 + R;
+    return (bytes + 15) / 16 * 16;
+}
+
+template <bool SOURCE, bool ONE, bool EXACT, bool BANK, bool REC>
+__global__ void __launch_bounds__(512) ev_pass(EvArgs a, int pass, uint32_t K) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ uint32_t s_scan[33];
+    __shared__ unsigned long long s_base;
+    TView t;
+    if (ONE) {
+        const EvInst& I = a.inst[0];
+        const uint32_t M = I.M, G = I.G, R = I.R, NB = I.nbins;
+        float* f = reinterpret_cast<float*>(smem);
+        float* s_xs = f;                 f += M * G * 4;
+        float* s_scdf = f;               f += M * G * G;
+        float* s_chi = f;                f += M * G;
+        float* s_maj = f;                f += 2 * G;
+        float* s_left = f;               f += R + 1;
+        float* s_invdx = f;              f += R;
+        uint32_t* s_first = reinterpret_cast<uint32_t*>(f);  f += R;
+        uint32_t* s_ncell = reinterpret_cast<uint32_t*>(f);  f += R;
+        uint16_t* s_grid = reinterpret_cast<uint16_t*>(f);
+        uint8_t* s_rmat = reinterpret_cast<uint8_t*>(s_grid + NB);
+        for (uint32_t i = threadIdx.x; i < M * G * 4; i += blockDim.x) s_xs[i] = I.xs[i];
+        for (uint32_t i = threadIdx.x; i < M * G * G; i += blockDim.x) s_scdf[i] = I.scdf[i];
+        for (uint32_t i = threadIdx.x; i < M * G; i += blockDim.x) s_chi[i] = I.chicdf[i];
+        for (uint32_t i = threadIdx.x; i < 2 * G; i += blockDim.x) s_maj[i] = I.maj[i];
+        for (uint32_t i = threadIdx.x; i < R + 1; i += blockDim.x) s_left[i] = I.rleft[i];
+        for (uint32_t i = threadIdx.x; i < R; i += blockDim.x) {
+            s_invdx[i] = I.rinvdx[i]; s_first[i] = I.rfirst[i]; s_ncell[i] = I.rncell[i];
+        }
+        for (uint32_t i = threadIdx.x; i < NB; i += blockDim.x) s_grid[i] = I.grid[i];
+        for (uint32_t i = threadIdx.x; i < R; i += blockDim.x) s_rmat[i] = I.rmat[i];
+        __syncthreads();
+        t.xs = s_xs; t.scdf = s_scdf; t.chi = s_chi; t.maj = s_maj; t.left = s_left;
+        t.grid = s_grid; t.rmat = s_rmat; t.invdx = s_invdx; t.first = s_first; t.ncell = s_ncell;
+        t.G = G; t.R = R; t.nbins = NB; t.L = I.L; t.inv_binw = I.inv_binw;
+        t.boundl = I.boundl; t.boundr = I.boundr;
+    }
+    const int qin = (pass - 1) & 1, qout = pass & 1;
+    const uint64_t n_in = SOURCE ? a.n_total : a.qcount[pass - 1];
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    const uint64_t trips = (n_in + stride - 1) / stride;
+    Acc acc = {0, 0, 0, 0, 0, 0};
+    for (uint64_t tr = 0; tr < trips; ++tr) {
+        uint64_t idx = tr * stride + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+        bool alive = false;
+        Part p;
+        if (idx < n_in) {
+            if (SOURCE) {
+                uint32_t inst = 0;
+                if (!ONE) {
+                    uint32_t lo = 0, hi = a.n_inst;        /* last begin <= idx */
+                    while (hi - lo > 1) {
+                        uint32_t mid = (lo + hi) >> 1;
+                        if (a.inst_begin[mid] <= idx) lo = mid; else hi = mid;
+                    }
+                    inst = lo;
+                }
+                const EvInst& I = a.inst[inst];
+                const GenState* st = I.st;
+                p.id = (uint32_t)idx;
+                p.inst = inst;
+                p.local = (uint32_t)(idx - I.hist_begin);
+                p.seq = 0;
+                p.rng = nr_pcg32_seeded(nr_generation_seed(I.seed, st->gen), p.local);
+                uint64_t nb = BANK ? st->n_bank : 0;
+                if (nb > 0) {
+                    const nraps_site* bank = I.bank[st->gen & 1];
+                    uint64_t j = ((uint64_t)p.local * nb) / I.N;
+                    nraps_site s = bank[j];
+                    p.x = s.x; p.g = s.group;
+                    p.mu = __fsub_rn(__fmul_rn(2.0f, u24(nr_pcg32_next(&p.rng))), 1.0f);
+                } else {
+                    uint32_t cell = I.fuel[((uint64_t)nr_pcg32_next(&p.rng) * I.nfuel) >> 32];
+                    float sub = u24(nr_pcg32_next(&p.rng));
+                    p.x = __fadd_rn(I.cleft[cell], __fmul_rn(sub, I.cdx[cell]));
+                    p.mu = __fsub_rn(__fmul_rn(2.0f, u24(nr_pcg32_next(&p.rng))), 1.0f);
+                    p.g = chi_group(I.chicdf + (uint32_t)I.cmat[cell] * I.G, I.G, u24(nr_pcg32_next(&p.rng)));
+                }
+                if (REC && inst == 0) a.rec[p.local].draws += (nb > 0) ? 1 : 4;
+            } else {
+                p.x = a.qx[qin][idx];
+                p.mu = a.qmu[qin][idx];
+                p.rng.state = a.qrng[qin][idx];
+                p.id = a.qid[qin][idx];
+                uint32_t pk = a.qpk[qin][idx];
+                p.g = pk & 15u;
+                p.inst = (pk >> 4) & 0xFFFu;
+                p.seq = pk >> 16;
+                const EvInst& I = a.inst[ONE ? 0 : p.inst];
+                p.local = (uint32_t)(p.id - I.hist_begin);
+                p.rng.inc = ((uint64_t)p.local << 1) | 1ULL;
+            }
+            const EvInst& I = a.inst[ONE ? 0 : p.inst];
+            TView tv = ONE ? t : global_view(I);
+            float inv_k = BANK ? I.st->inv_kf : 0.0f;
+            unsigned long long kq_part = 0;
+            alive = run_particle<EXACT, BANK, REC>(a, I, tv, p, K, inv_k, acc, kq_part);
+            if (!ONE && kq_part) atomicAdd(&I.st->kq, kq_part);
+        }
+        /* compact survivors into the out queue */
+        uint32_t excl;
+        uint32_t total = nrdev::block_excl_scan(alive ? 1u : 0u, &excl, s_scan);
+        if (total) {
+            if (threadIdx.x == 0) s_base = atomicAdd(&a.qcount[pass], (unsigned long long)total);
+            __syncthreads();
+            if (alive) {
+                uint64_t o = s_base + excl;
+                a.qx[qout][o] = p.x;
+                a.qmu[qout][o] = p.mu;
+                a.qrng[qout][o] = p.rng.state;
+                a.qid[qout][o] = p.id;
+                a.qpk[qout][o] = p.g | (p.inst << 4) | (p.seq << 16);
+            }
+            __syncthreads();
+        }
+    }
+    /* flush counters: one atomic per warp */
+    unsigned long long kq = nrdev::warp_sum_u64(ONE ? acc.kq : 0ull);
+    unsigned long long coll = nrdev::warp_sum_u64(acc.coll), virt = nrdev::warp_sum_u64(acc.virt);
+    unsigned long long ab = nrdev::warp_sum_u64(acc.absorbed), lk = nrdev::warp_sum_u64(acc.leaked);
+    unsigned long long cp = nrdev::warp_sum_u64(acc.capped);
+    if ((threadIdx.x & 31) == 0) {
+        GenState* s = a.stats;
+        if (ONE && kq) atomicAdd(&a.inst[0].st->kq, kq);
+        if (coll) atomicAdd(&s->collisions, coll);
+        if (virt) atomicAdd(&s->virtual_collisions, virt);
+        if (ab) atomicAdd(&s->absorbed, ab);
+        if (lk) atomicAdd(&s->leaked, lk);
+        if (cp) atomicAdd(&s->capped, cp);
+    }
+}
+
+__device__ __forceinline__ uint32_t find_inst(const uint64_t* begin, uint32_t n, uint64_t i) {
+    uint32_t lo = 0, hi = n;
+    while (hi - lo > 1) {
+        uint32_t mid = (lo + hi) >> 1;
+        if (begin[mid] <= i) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+/* ordered bank: site (parent, seq) -> offsets[parent] + seq - offsets[first history of its instance] */
+__global__ void ev_scatter(EvArgs a) {
+    const uint32_t slab = blockIdx.x % NSLAB;
+    const uint64_t per = gridDim.x / NSLAB;
+    uint64_t filled = a.slab_count[slab];
+    if (filled > a.slab_cap) filled = a.slab_cap;
+    for (uint64_t j = (uint64_t)(blockIdx.x / NSLAB) * blockDim.x + threadIdx.x; j < filled;
+         j += per * blockDim.x) {
+        uint64_t i = (uint64_t)slab * a.slab_cap + j;
+        uint32_t gi = a.sgi[i];
+        uint32_t inst = gi >> 4;
+        const EvInst& I = a.inst[inst];
+        uint64_t pos = (uint64_t)a.offsets[a.sparent[i]] + a.sseq[i] - a.offsets[I.hist_begin];
+        if (pos < I.bank_cap) {
+            nraps_site s;
+            s.x = a.sx[i];
+            s.cell = a.scell[i];
+            s.group = gi & 15u;
+            s.pad = 0;
+            I.bank[(I.st->gen + 1) & 1][pos] = s;
+            atomicAdd(&I.hist[s.cell], 1u);
+        }
+    }
+}
+
+/* one thread per (instance, cell): reads and clears the G tally bins */
+__global__ void ev_fin_bins(EvArgs a) {
+    for (uint64_t gc = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; gc < a.n_cells_total;
+         gc += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t inst = a.n_inst == 1 ? 0u : find_inst(a.cell_begin, a.n_inst, gc);
+        const EvInst& I = a.inst[inst];
+        const GenState* st = I.st;
+        uint64_t c = gc - I.cell_begin;
+        const uint64_t gen = st->gen;
+        if (gen >= I.generations) continue;
+        const bool active = gen >= I.skip;
+        const double fund = 1.0 / (double)(I.generations - I.skip);
+        const double k = st->k;
+        const double conversion = I.conv_const * k;
+        const double N = (double)I.N;
+        double dx = I.dx64[c];
+        uint32_t m = I.cmat[c];
+        double fs = 0.0;
+        for (uint32_t g = 0; g < I.G; ++g) {
+            uint64_t bin = (uint64_t)g * I.nc + c;
+            double tl = I.tally[bin];
+            I.tally[bin] = 0.0;
+            double flux = tl / (k * N * dx);
+            fs += I.nsf64[m + (uint64_t)I.M * g] * flux;
+            double phi = tl / (N * dx);
+            if (active) {
+                I.flux_acc[bin] += flux * conversion * fund;
+                I.flux_sum[bin] += phi;
+                I.flux_sq[bin] += phi * phi;
+            }
+        }
+        if (active) I.fs_acc[c] += fs * fund;
+        if (a.bank) {
+            uint32_t cnt = I.hist[c];
+            I.hist[c] = 0;
+            uint64_t B = a.offsets[I.hist_begin + I.N] - a.offsets[I.hist_begin];
+            if (cnt && B) {
+                double pr = (double)cnt / (double)B;
+                atomicAdd(&I.st->h_acc, -pr * nr_log(pr) * 1.4426950408889634);
+            }
+        }
+    }
+}
+
+__global__ void ev_fin_state(EvArgs a) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) {
+        for (uint32_t p = 0; p < MAX_PASSES + 2; ++p) a.qcount[p] = 0;
+        for (uint32_t s = 0; s < NSLAB; ++s) a.slab_count[s] = 0;
+        if (a.n_inst > 1) {
+            GenState* s = a.stats;
+            s->tot_collisions += s->collisions; s->tot_virtual += s->virtual_collisions;
+            s->tot_absorbed += s->absorbed; s->tot_leaked += s->leaked; s->tot_capped += s->capped;
+            s->collisions = s->virtual_collisions = s->absorbed = s->leaked = s->capped = 0;
+        }
+    }
+    if (i >= a.n_inst) return;
+    const EvInst& I = a.inst[i];
+    GenState* st = I.st;
+    uint64_t gen = st->gen;
+    if (gen >= I.generations) return;
+    double k_new = nr_unfix(st->kq) / (double)I.N;
+    I.k64[gen] = k_new;
+    I.entropy[gen] = a.bank ? st->h_acc : 0.0;
+    if (a.bank) {
+        unsigned long long B = a.offsets[I.hist_begin + I.N] - a.offsets[I.hist_begin];
+        st->tot_sites += B;
+        if (B > I.bank_cap) { B = I.bank_cap; st->error |= NR_ERR_CAPACITY; }
+        st->n_bank = B;
+        if (B == 0) st->error |= NR_ERR_EMPTY;
+    }
+    if (a.n_inst == 1) {
+        st->tot_collisions += st->collisions; st->tot_virtual += st->virtual_collisions;
+        st->tot_absorbed += st->absorbed; st->tot_leaked += st->leaked; st->tot_capped += st->capped;
+        st->collisions = st->virtual_collisions = st->absorbed = st->leaked = st->capped = 0;
+    }
+    st->tot_histories += I.N;
+    st->kq = 0;
+    st->h_acc = 0.0;
+    st->n_sites = 0;
+    st->k = k_new;
+    st->inv_kf = (float)(1.0 / k_new);
+    st->gen = gen + 1;
+}
+
+template <class T> struct DBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    ~DBuf() { if (p) cudaFree(p); }
+    cudaError_t alloc(size_t count) {
+        if (p) { cudaFree(p); p = nullptr; }
+        n = count;
+        return count ? cudaMalloc(&p, count * sizeof(T)) : cudaSuccess;
+    }
+};
+
+}  // namespace
+
+struct EventEngine::Impl {
+    struct Inst {
+        EvHostTables h;
+        DBuf<unsigned char> blob;
+        EvInst d{};
+        EvBuffers b{};
+    };
+    std::vector<Inst*> inst;
+    int mode = NRAPS_MODE_BANK;
+    bool exact = false;
+    uint64_t max_events = 1ULL << 24;
+    DBuf<EvInst> d_inst;
+    DBuf<uint64_t> d_inst_begin, d_cell_begin;
+    DBuf<float> qx[2], qmu[2];
+    DBuf<unsigned long long> qrng[2];
+    DBuf<uint32_t> qid[2], qpk[2];
+    DBuf<unsigned long long> qcount, slab_count;
+    DBuf<float> sx;
+    DBuf<uint32_t> scell, sgi, sparent, sseq, count, offsets, block_sums;
+    DBuf<GenState> bstats;
+    uint64_t n_total = 0, n_cells_total = 0, slab_cap = 0;
+    nraps_history_record* rec = nullptr;
+    EvArgs args{};
+    bool committed = false;
+    int grid_blocks = 0;
+    size_t smem_bytes = 0;
+    bool one = true;
+    ~Impl() { for (Inst* i : inst) delete i; }
+};
+
+EventEngine::EventEngine() : impl_(new Impl()) {}
+EventEngine::~EventEngine() { delete impl_; }
+
+int EventEngine::configure(const nraps_opts& o, std::string& err) {
+    if (o.mode != NRAPS_MODE_PHYSICS && o.mode != NRAPS_MODE_BANK) { err = "WOODCOCK runs PHYSICS or BANK mode"; return NRAPS_ERR_INVALID; }
+    impl_->mode = o.mode;
+    impl_->exact = o.exact_log != 0;
+    impl_->max_events = o.max_events ? o.max_events : (1ULL << 24);
+    if (o.block_size) params.block = o.block_size;
+    if (o.events_per_pass) params.K = o.events_per_pass;
+    if (o.passes) params.passes = o.passes;
+    if (params.block != 128 && params.block != 256 && params.block != 512) { err = "block_size must be 128, 256 or 512"; return NRAPS_ERR_INVALID; }
+    if (params.passes < 1 || params.passes > MAX_PASSES) { err = "passes must be in [1, 16]"; return NRAPS_ERR_INVALID; }
+    if (params.K < 1) { err = "events_per_pass must be >= 1"; return NRAPS_ERR_INVALID; }
+    impl_->committed = false;
+    return NRAPS_OK;
+}
+
+uint64_t EventEngine::table_bytes(const nraps_problem& p) {
+    uint64_t M = p.variables.mattypes, G = p.variables.energygroups, nc = p.mesh.n_cells;
+    return (M * G * (4 + G + 1) + 2 * G) * 4 + nc * (4 + 4 + 1 + 8) + M * G * 8 + p.n_fuel * 4 +
+           nc * (4 + 4 + 4 + 4 + 1) + 16384 * 2 + 16 * 256;
+}
+
+int EventEngine::add_instance(const nraps_problem& p, const EvBuffers& b, std::string& err) {
+    if (impl_->inst.size() >= 4095) { err = "at most 4095 instances per batch"; return -1; }
+    Impl::Inst* in = new Impl::Inst();
+    if (build_event_tables(p, in->h, err)) { delete in; return -1; }
+    const EvHostTables& h = in->h;
+    size_t off = 0;
+    auto take = [&](size_t bytes) { size_t o = off; off = (off + bytes + 255) & ~(size_t)255; return o; };
+    size_t o_xs = take(h.xs.size() * 4), o_scdf = take(h.scdf.size() * 4), o_chi = take(h.chicdf.size() * 4);
+    size_t o_maj = take(h.maj.size() * 4), o_left = take(h.rleft.size() * 4), o_invdx = take(h.rinvdx.size() * 4);
+    size_t o_rmat = take(h.rmat.size()), o_rfirst = take(h.rfirst.size() * 4), o_rn = take(h.rncell.size() * 4);
+    size_t o_grid = take(h.grid.size() * 2), o_fuel = take(h.fuel.size() * 4), o_cleft = take(h.cleft.size() * 4);
+    size_t o_cdx = take(h.cdx.size() * 4), o_cmat = take(h.cmat.size()), o_nsf = take(h.nsf64.size() * 8);
+    size_t o_dx = take(h.dx64.size() * 8);
+    std::vector<unsigned char> host(off, 0);
+    auto put = [&](size_t o, const void* src, size_t bytes) { if (bytes) std::memcpy(host.data() + o, src, bytes); };
+    put(o_xs, h.xs.data(), h.xs.size() * 4); put(o_scdf, h.scdf.data(), h.scdf.size() * 4);
+    put(o_chi, h.chicdf.data(), h.chicdf.size() * 4); put(o_maj, h.maj.data(), h.maj.size() * 4);
+    put(o_left, h.rleft.data(), h.rleft.size() * 4); put(o_invdx, h.rinvdx.data(), h.rinvdx.size() * 4);
+    put(o_rmat, h.rmat.data(), h.rmat.size()); put(o_rfirst, h.rfirst.data(), h.rfirst.size() * 4);
+    put(o_rn, h.rncell.data(), h.rncell.size() * 4); put(o_grid, h.grid.data(), h.grid.size() * 2);
+    put(o_fuel, h.fuel.data(), h.fuel.size() * 4); put(o_cleft, h.cleft.data(), h.cleft.size() * 4);
+    put(o_cdx, h.cdx.data(), h.cdx.size() * 4); put(o_cmat, h.cmat.data(), h.cmat.size());
+    put(o_nsf, h.nsf64.data(), h.nsf64.size() * 8); put(o_dx, h.dx64.data(), h.dx64.size() * 8);
+    cudaError_t e = in->blob.alloc(off);
+    if (e == cudaSuccess) e = cudaMemcpy(in->blob.p, host.data(), off, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) { err = std::string("event tables: ") + cudaGetErrorString(e); delete in; return -1; }
+    unsigned char* B = in->blob.p;
+    EvInst& d = in->d;
+    d.xs = (const float*)(B + o_xs); d.scdf = (const float*)(B + o_scdf); d.chicdf = (const float*)(B + o_chi);
+    d.maj = (const float*)(B + o_maj); d.rleft = (const float*)(B + o_left); d.rinvdx = (const float*)(B + o_invdx);
+    d.rmat = B + o_rmat; d.rfirst = (const uint32_t*)(B + o_rfirst); d.rncell = (const uint32_t*)(B + o_rn);
+    d.grid = (const uint16_t*)(B + o_grid); d.fuel = (const uint32_t*)(B + o_fuel);
+    d.cleft = (const float*)(B + o_cleft); d.cdx = (const float*)(B + o_cdx); d.cmat = B + o_cmat;
+    d.nsf64 = (const double*)(B + o_nsf); d.dx64 = (const double*)(B + o_dx);
+    d.M = h.M; d.G = h.G; d.R = h.R; d.nc = h.nc; d.nbins = h.nbins; d.nfuel = h.nfuel;
+    d.L = h.L; d.inv_binw = h.inv_binw; d.boundl = h.boundl; d.boundr = h.boundr;
+    d.N = p.variables.histories; d.seed = b.seed;
+    d.st = b.st; d.tally = b.tally;
+    d.flux_acc = b.flux_acc; d.fs_acc = b.fs_acc; d.flux_sum = b.flux_sum; d.flux_sq = b.flux_sq;
+    d.k64 = b.k64; d.entropy = b.entropy;
+    d.bank[0] = b.bank[0]; d.bank[1] = b.bank[1]; d.bank_cap = b.bank_cap; d.hist = b.hist;
+    d.generations = b.generations; d.skip = b.skip; d.conv_const = h.conv_const;
+    in->b = b;
+    impl_->inst.push_back(in);
+    impl_->committed = false;
+    return (int)impl_->inst.size() - 1;
+}
+
+void EventEngine::clear_instances() {
+    for (auto* i : impl_->inst) delete i;
+    impl_->inst.clear();
+    impl_->committed = false;
+}
+
+uint32_t EventEngine::n_instances() const { return (uint32_t)impl_->inst.size(); }
+void EventEngine::set_records(nraps_history_record* rec) { impl_->rec = rec; impl_->committed = false; }
+const uint32_t* EventEngine::offsets() const { return impl_->offsets.p; }
+uint64_t EventEngine::n_total() const { return impl_->n_total; }
+GenState* EventEngine::batch_stats() const { return impl_->bstats.p; }
+
+uint64_t EventEngine::shared_bytes() const {
+    const Impl* m = impl_;
+    return m->n_total * (24 * 2 + 8) + NSLAB * m->slab_cap * 20;
+}
+
+namespace {
+template <bool SOURCE, bool ONE, bool EXACT, bool BANK, bool REC>
+void set_smem_attr(size_t smem) {
+    static size_t granted = 48 * 1024;          /* default dynamic limit */
+    if (smem > granted) {
+        cudaFuncSetAttribute(ev_pass<SOURCE, ONE, EXACT, BANK, REC>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        granted = smem;
+    }
+}
+
+template <bool ONE, bool EXACT, bool BANK, bool REC>
+int launch_passes(const EvArgs& a, const EvParams& prm, int grid, size_t smem, uint64_t n_total,
+                  cudaStream_t s) {
+    int launched = 0;
+    uint32_t block = prm.block;
+    unsigned g0 = (unsigned)std::min<uint64_t>((n_total + block - 1) / block, (uint64_t)grid);
+    if (g0 == 0) g0 = 1;
+    set_smem_attr<true, ONE, EXACT, BANK, REC>(smem);
+    set_smem_attr<false, ONE, EXACT, BANK, REC>(smem);
+    uint32_t P = prm.passes;
+    ev_pass<true, ONE, EXACT, BANK, REC><<<g0, block, smem, s>>>(a, 0, P == 0 ? 0xFFFFFFFFu : prm.K);
+    ++launched;
+    for (uint32_t p = 1; p <= P; ++p) {
+        uint32_t K = (p == P) ? 0xFFFFFFFFu : prm.K;
+        ev_pass<false, ONE, EXACT, BANK, REC><<<(unsigned)grid, block, smem, s>>>(a, (int)p, K);
+        ++launched;
+    }
+    return cudaPeekAtLastError() == cudaSuccess ? launched : -1;
+}
+}  // namespace
+
+int EventEngine::commit(cudaStream_t s, std::string& err) {
+    Impl& m = *impl_;
+    if (m.inst.empty()) { err = "no instances"; return NRAPS_ERR_INVALID; }
+    uint32_t n = (uint32_t)m.inst.size();
+    std::vector<uint64_t> ib(n + 1, 0), cb(n + 1, 0);
+    for (uint32_t i = 0; i < n; ++i) {
+        ib[i + 1] = ib[i] + m.inst[i]->d.N;
+        cb[i + 1] = cb[i] + m.inst[i]->d.nc;
+        m.inst[i]->d.hist_begin = ib[i];
+        m.inst[i]->d.cell_begin = cb[i];
+    }
+    if (ib[n] >= (1ULL << 32)) { err = "at most 2^32-1 particles per batch generation"; return NRAPS_ERR_INVALID; }
+    bool bank = m.mode == NRAPS_MODE_BANK;
+    uint64_t old_total = m.n_total;
+    m.n_total = ib[n];
+    m.n_cells_total = cb[n];
+    std::vector<EvInst> d(n);
+    uint64_t bank_sum = 0;
+    for (uint32_t i = 0; i < n; ++i) { d[i] = m.inst[i]->d; bank_sum += m.inst[i]->b.bank_cap; }
+    cudaError_t e = cudaSuccess;
+    auto A = [&](cudaError_t x) { if (e == cudaSuccess) e = x; };
+    if (m.d_inst.n < n) A(m.d_inst.alloc(n));
+    if (m.d_inst_begin.n < n + 1) { A(m.d_inst_begin.alloc(n + 1)); A(m.d_cell_begin.alloc(n + 1)); }
+    A(cudaMemcpyAsync(m.d_inst.p, d.data(), n * sizeof(EvInst), cudaMemcpyHostToDevice, s));
+    A(cudaMemcpyAsync(m.d_inst_begin.p, ib.data(), (n + 1) * 8, cudaMemcpyHostToDevice, s));
+    A(cudaMemcpyAsync(m.d_cell_begin.p, cb.data(), (n + 1) * 8, cudaMemcpyHostToDevice, s));
+    if (m.n_total > old_total || !m.qx[0].p) {
+        for (int q = 0; q < 2; ++q) {
+            A(m.qx[q].alloc(m.n_total)); A(m.qmu[q].alloc(m.n_total)); A(m.qrng[q].alloc(m.n_total));
+            A(m.qid[q].alloc(m.n_total)); A(m.qpk[q].alloc(m.n_total));
+        }
+        A(m.count.alloc(m.n_total)); A(m.offsets.alloc(m.n_total + 1));
+        A(m.block_sums.alloc((m.n_total + 4095) / 4096 + 1));
+    }
+    if (!m.qcount.p) { A(m.qcount.alloc(MAX_PASSES + 2)); A(m.slab_count.alloc(NSLAB)); A(m.bstats.alloc(1)); }
+    uint64_t want_slab = bank ? (bank_sum + 2 * m.n_total) / NSLAB + 4096 : 1;
+    if (want_slab > m.slab_cap || !m.sx.p) {
+        m.slab_cap = want_slab;
+        uint64_t tot = NSLAB * m.slab_cap;
+        A(m.sx.alloc(tot)); A(m.scell.alloc(tot)); A(m.sgi.alloc(tot)); A(m.sparent.alloc(tot)); A(m.sseq.alloc(tot));
+    }
+    A(cudaMemsetAsync(m.qcount.p, 0, (MAX_PASSES + 2) * 8, s));
+    A(cudaMemsetAsync(m.slab_count.p, 0, NSLAB * 8, s));
+    A(cudaMemsetAsync(m.bstats.p, 0, sizeof(GenState), s));
+    if (bank) A(cudaMemsetAsync(m.count.p, 0, m.n_total * 4, s));
+    if (e != cudaSuccess) { err = std::string("event engine buffers: ") + cudaGetErrorString(e); return NRAPS_ERR_NOMEM; }
+    EvArgs& a = m.args;
+    a.inst = m.d_inst.p; a.n_inst = n; a.inst_begin = m.d_inst_begin.p; a.cell_begin = m.d_cell_begin.p;
+    a.n_total = m.n_total; a.n_cells_total = m.n_cells_total;
+    for (int q = 0; q < 2; ++q) {
+        a.qx[q] = m.qx[q].p; a.qmu[q] = m.qmu[q].p; a.qrng[q] = m.qrng[q].p; a.qid[q] = m.qid[q].p; a.qpk[q] = m.qpk[q].p;
+    }
+    a.qcount = m.qcount.p;
+    a.sx = m.sx.p; a.scell = m.scell.p; a.sgi = m.sgi.p; a.sparent = m.sparent.p; a.sseq = m.sseq.p;
+    a.slab_count = m.slab_count.p; a.slab_cap = m.slab_cap;
+    a.count = m.count.p; a.offsets = m.offsets.p;
+    a.stats = (n == 1) ? m.inst[0]->d.st : m.bstats.p;
+    a.max_events = m.max_events;
+    a.rec = m.rec;
+    a.bank = bank ? 1 : 0;
+    /* one instance with tables that fit: stage them in shared memory */
+    m.one = false;
+    m.smem_bytes = 0;
+    if (n == 1) {
+        const EvInst& I = m.inst[0]->d;
+        size_t sb = smem_words(I.M, I.G, I.R, I.nbins);
+        if (sb <= 160 * 1024) { m.one = true; m.smem_bytes = sb; }
+    }
+    m.committed = true;
+    return size_grid();
+}
+
+int EventEngine::size_grid() {
+    Impl& m = *impl_;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    /* persistent grid: as many blocks as are resident at once */
+    int per_sm = 0;
+    const void* fn = m.one ? (m.exact ? (const void*)ev_pass<false, true, true, true, false>
+                                      : (const void*)ev_pass<false, true, false, true, false>)
+                           : (const void*)ev_pass<false, false, false, true, false>;
+    if (m.one && m.smem_bytes > 48 * 1024)
+        cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)m.smem_bytes);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, (int)params.block,
+                                                      m.one ? m.smem_bytes : 0) != cudaSuccess || per_sm < 1)
+        per_sm = 1;
+    m.grid_blocks = sms * per_sm;
+    return NRAPS_OK;
+}
+
+
+
+uint64_t EventEngine::launches_per_generation() const { return 1 + params.passes; }
+
+int EventEngine::enqueue_generation(cudaStream_t s, bool with_finalize, cudaEvent_t t0, cudaEvent_t t1) {
+    Impl& m = *impl_;
+    if (!m.committed) return -1;
+    if (t0) cudaEventRecord(t0, s);
+    const EvArgs& a = m.args;
+    bool bank = m.mode == NRAPS_MODE_BANK;
+    bool rec = m.rec != nullptr;
+    int r;
+#define EV_LAUNCH(ONE, EXACT, BANK, REC) \
+    r = launch_passes<ONE, EXACT, BANK, REC>(a, params, m.grid_blocks, ONE ? m.smem_bytes : 0, m.n_total, s)
+    if (rec) {
+        if (bank) { if (m.exact) EV_LAUNCH(true, true, true, true); else EV_LAUNCH(true, false, true, true); }
+        else { if (m.exact) EV_LAUNCH(true, true, false, true); else EV_LAUNCH(true, false, false, true); }
+    } else if (m.one) {
+        if (bank) { if (m.exact) EV_LAUNCH(true, true, true, false); else EV_LAUNCH(true, false, true, false); }
+        else { if (m.exact) EV_LAUNCH(true, true, false, false); else EV_LAUNCH(true, false, false, false); }
+    } else {
+        if (bank) { if (m.exact) EV_LAUNCH(false, true, true, false); else EV_LAUNCH(false, false, true, false); }
+        else { if (m.exact) EV_LAUNCH(false, true, false, false); else EV_LAUNCH(false, false, false, false); }
+    }
+#undef EV_LAUNCH
+    if (r < 0) return -1;
+    if (t1) cudaEventRecord(t1, s);
+    int n = r;
+    if (bank) {
+        int q = launch_exclusive_scan(m.count.p, m.n_total, m.block_sums.p, m.offsets.p, nullptr, s);
+        if (q < 0) return -1;
+        n += q;
+        ev_scatter<<<NSLAB * 8, 256, 0, s>>>(a);
+        ++n;
+    }
+    if (with_finalize) {
+        unsigned gb = (unsigned)std::min<uint64_t>((m.n_cells_total + 255) / 256, (uint64_t)m.grid_blocks * 2);
+        ev_fin_bins<<<gb ? gb : 1, 256, 0, s>>>(a);
+        ev_fin_state<<<(a.n_inst + 127) / 128, 128, 0, s>>>(a);
+        n += 2;
+    }
+    return cudaPeekAtLastError() == cudaSuccess ? n : -1;
+}

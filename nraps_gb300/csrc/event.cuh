@@ -1,25 +1,86 @@
 /*
- * event.cuh — the event-based Woodcock (delta-tracking) transport engine.
+ * event.cuh — event-based Woodcock (delta-tracking) transport engine.
+ *
+ * One engine runs one generation of every problem instance it holds in a
+ * fixed sequence of launches:
+ *   pass 0      every source particle is born (from its instance's ordered
+ *               fission bank, or the uniform fuel source) and runs up to K
+ *               real collisions; survivors are compacted into queue 0;
+ *   pass 1..P-1 the queued particles run K more real collisions each and
+ *               the survivors are compacted into the other queue;
+ *   drain       the last queue runs to completion;
+ *   bank        exclusive scan of per-history site counts, then the
+ *               unordered sites are scattered to (parent, sequence) order;
+ *   finalize    per-cell FP64 flux/fission-source accumulation, Shannon
+ *               entropy, and per-instance k, bank size and generation index.
+ * Every particle owns a PCG32 stream (seed of its instance and generation,
+ * stream = its history index within the instance), so the result does not
+ * depend on K, P, the block size, or which other instances share the batch.
  */
 #ifndef NRAPS_EVENT_CUH
 #define NRAPS_EVENT_CUH
 #include <string>
+#include <vector>
 
 #include "engine.cuh"
+
+/* Per-instance device buffers owned by the caller (a session or a batch). */
+struct EvBuffers {
+    GenState* st;
+    double* tally;                         /* G*nc                          */
+    double *flux_acc, *fs_acc, *flux_sum, *flux_sq;
+    double *k64, *entropy;                 /* generations                    */
+    nraps_site* bank[2];                   /* BANK mode ordered banks        */
+    uint64_t bank_cap;
+    uint32_t* hist;                        /* nc (BANK mode)                 */
+    uint64_t generations, skip;
+    uint64_t seed;
+};
+
+struct EvParams {
+    uint32_t block = 256;   /* threads per block of the transport passes       */
+    uint32_t K = 4;         /* real collisions per particle per queue pass     */
+    uint32_t passes = 3;    /* queue passes before the drain pass (>= 1)       */
+};
 
 class EventEngine {
 public:
     EventEngine();
     ~EventEngine();
-    /* Build device tables and particle queues for one problem. */
-    int init(const nraps_problem& p, const nraps_opts& o, GenState* st, double* tally,
-             SiteSink sink, nraps_site* bank0, nraps_site* bank1, cudaStream_t s, std::string& err);
-    /* Enqueue one generation's transport; returns kernels launched, <0 on error. */
-    int enqueue_generation(cudaStream_t s);
-    uint64_t launches_per_generation() const;
+    EventEngine(const EventEngine&) = delete;
+    EventEngine& operator=(const EventEngine&) = delete;
 
-private:
+    /* mode (PHYSICS/BANK), exact_log, max_events; keeps the instances. */
+    int configure(const nraps_opts& o, std::string& err);
+    /* Build tables for one problem; returns the instance index, or -1. */
+    int add_instance(const nraps_problem& p, const EvBuffers& b, std::string& err);
+    void clear_instances();
+    uint32_t n_instances() const;
+    /* Upload descriptors and size the shared queues/site slabs. */
+    int commit(cudaStream_t s, std::string& err);
+    /* One generation of every instance; returns kernels launched, <0 on error. */
+    int enqueue_generation(cudaStream_t s, bool with_finalize = true, cudaEvent_t t0 = nullptr,
+                           cudaEvent_t t1 = nullptr);
+    uint64_t launches_per_generation() const;
+    /* Per-history records of instance 0 (trace), or nullptr. */
+    void set_records(nraps_history_record* rec);
+    /* Device scan offsets (n_total+1) of the last generation, for traces. */
+    const uint32_t* offsets() const;
+    uint64_t n_total() const;
+    /* Batch-level counters (collisions etc.) when the engine has several
+       instances; a single instance counts into its own GenState. */
+    GenState* batch_stats() const;
+    /* Device bytes of the shared (per-generation) buffers. */
+    uint64_t shared_bytes() const;
+    /* Device bytes one instance's tables need. */
+    static uint64_t table_bytes(const nraps_problem& p);
+
+    EvParams params;
+    /* Size the persistent grid for the current params (after a change). */
+    int size_grid();
+
     struct Impl;
+private:
     Impl* impl_;
 };
 #endif

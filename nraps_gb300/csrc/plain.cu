@@ -21,6 +21,7 @@
  */
 #include "engine.cuh"
 #include "nr_math.h"
+#include "dev_util.cuh"
 
 namespace {
 
@@ -47,16 +48,7 @@ struct Counters {
     uint32_t coll, cross, absorbed, leaked, capped;
 };
 
-/* warp-aggregated increment of a 64-bit counter by 1 for each calling lane */
-__device__ __forceinline__ unsigned long long agg_inc(unsigned long long* ctr) {
-    unsigned mask = __activemask();
-    int lane = threadIdx.x & 31;
-    int leader = __ffs(mask) - 1;
-    unsigned long long base = 0;
-    if (lane == leader) base = atomicAdd(ctr, (unsigned long long)__popc(mask));
-    base = __shfl_sync(mask, base, leader);
-    return base + (unsigned long long)__popc(mask & ((1u << lane) - 1u));
-}
+using nrdev::agg_inc;
 
 /* Rust partition_point, fixed-iteration form, deterministic predicate x < v */
 template <class T>

@@ -10,6 +10,7 @@
 #include "tables.hpp"
 
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 
 namespace {
@@ -89,3 +90,117 @@ int build_tables(const nraps_problem& p, std::vector<unsigned char>& blob, Table
 
 template int build_tables<float>(const nraps_problem&, std::vector<unsigned char>&, TableLayout&, std::string&);
 template int build_tables<double>(const nraps_problem&, std::vector<unsigned char>&, TableLayout&, std::string&);
+
+int build_event_tables(const nraps_problem& p, EvHostTables& t, std::string& err) {
+    const nraps_variables& v = p.variables;
+    const uint64_t M = v.mattypes, G = v.energygroups, nc = p.mesh.n_cells;
+    if (M == 0 || G == 0 || nc == 0) { err = "empty problem (mattypes, energygroups or cells is 0)"; return 1; }
+    if (G > 16) { err = "at most 16 energy groups are supported"; return 1; }
+    if (M > 255) { err = "at most 255 materials are supported"; return 1; }
+    if (nc >= (1ULL << 27)) { err = "at most 2^27 cells are supported"; return 1; }
+    if (p.xsdata.n_xs < M * G || p.xsdata.n_scat < M * G * G) { err = "cross-section arrays shorter than MatTypes*EnergyGroups"; return 1; }
+    if (p.n_fuel == 0 || !p.fuel_indices) { err = "no fuel cells (fuel_indices is empty)"; return 1; }
+    t.M = (uint32_t)M; t.G = (uint32_t)G; t.nc = (uint32_t)nc; t.nfuel = (uint32_t)p.n_fuel;
+    t.boundl = v.boundl; t.boundr = v.boundr;
+    const nraps_xsdata& x = p.xsdata;
+    t.xs.assign(M * G * 4, 0.f);
+    std::vector<float> sigtr(M * G);
+    for (uint64_t m = 0; m < M; ++m)
+        for (uint64_t g = 0; g < G; ++g) {
+            uint64_t i = m + M * g;
+            float st = (float)((double)x.sigt[i] - (double)x.mu[i] * (double)x.sigs[i]);
+            sigtr[m * G + g] = st;
+            float* X = &t.xs[(m * G + g) * 4];
+            X[0] = st;
+            X[1] = st > 0.f ? x.siga[i] / st : 1.f;
+            X[2] = st > 0.f ? (x.nut[i] * x.sigf[i]) / st : 0.f;
+            X[3] = st > 0.f ? 1.0f / st : 0.f;
+        }
+    t.scdf.assign(M * G * G, 1.f);
+    for (uint64_t m = 0; m < M; ++m)
+        for (uint64_t g = 0; g < G; ++g) {
+            uint64_t i = m + M * g;
+            float cum[16]; float c = 0.f;
+            for (uint64_t e = 0; e < G; ++e) {
+                float s = x.scat_matrix[G * G * m + G * g + e];
+                if (e == g) s = s - x.mu[i] * x.sigs[i];
+                if (s < 0.f) s = 0.f;
+                c = c + s; cum[e] = c;
+            }
+            for (uint64_t e = 0; e < G; ++e) t.scdf[(m * G + g) * G + e] = (c > 0.f) ? cum[e] / c : 1.f;
+        }
+    t.chicdf.assign(M * G, 0.f);
+    for (uint64_t m = 0; m < M; ++m) {
+        float c = 0.f;
+        for (uint64_t g = 0; g < G; ++g) { c += x.chit[m + M * g]; t.chicdf[m * G + g] = c; }
+    }
+    /* regions */
+    t.rleft.clear(); t.rmat.clear(); t.rfirst.clear(); t.rncell.clear(); t.rinvdx.clear();
+    std::vector<bool> present(M, false);
+    for (uint64_t c = 0; c < nc; ++c) {
+        uint8_t m = p.mesh.matid[c];
+        if (m >= M) { err = "mesh matid out of range of MatTypes"; return 1; }
+        present[m] = true;
+        bool start = c == 0 || m != p.mesh.matid[c - 1] ||
+                     std::memcmp(&p.mesh.delta_x[c], &p.mesh.delta_x[c - 1], 4) != 0;
+        if (start) {
+            t.rleft.push_back(p.mesh.mesh_left[c]);
+            t.rmat.push_back(m);
+            t.rfirst.push_back((uint32_t)c);
+            t.rncell.push_back(1);
+            t.rinvdx.push_back((float)(1.0 / (double)p.mesh.delta_x[c]));
+        } else {
+            t.rncell.back()++;
+        }
+    }
+    t.R = (uint32_t)t.rmat.size();
+    if (t.R > 65535) { err = "at most 65535 material regions are supported"; return 1; }
+    t.rleft.push_back(p.mesh.mesh_right[nc - 1]);
+    t.L = t.rleft[t.R];
+    if (!(t.L > 0.f) || t.rleft[0] != 0.f) { err = "mesh must start at 0 and have positive length"; return 1; }
+    t.maj.assign(2 * G, 0.f);
+    for (uint64_t g = 0; g < G; ++g) {
+        float mj = 0.f;
+        for (uint64_t m = 0; m < M; ++m)
+            if (present[m]) {
+                if (!(sigtr[m * G + g] > 0.f)) { err = "sigt - mu*sigs must be positive for every material in the mesh"; return 1; }
+                mj = std::max(mj, sigtr[m * G + g]);
+            }
+        t.maj[g] = mj;
+        t.maj[G + g] = 1.0f / mj;
+    }
+    double wmin = 1e300;
+    for (uint32_t r = 0; r < t.R; ++r) {
+        double w = (double)t.rleft[r + 1] - (double)t.rleft[r];
+        if (!(w > 0.0)) { err = "material region of zero width"; return 1; }
+        wmin = std::min(wmin, w);
+    }
+    uint64_t want = (uint64_t)std::ceil(4.0 * (double)t.L / wmin);
+    uint32_t nb = 16;
+    while (nb < want && nb < 16384) nb <<= 1;
+    t.nbins = nb;
+    t.inv_binw = (float)((double)nb / (double)t.L);
+    t.grid.assign(nb, 0);
+    uint32_t r = 0;
+    for (uint32_t b = 0; b < nb; ++b) {
+        double xb = (double)b * (double)t.L / (double)nb;
+        while (r + 1 < t.R && (double)t.rleft[r + 1] <= xb) ++r;
+        t.grid[b] = (uint16_t)r;
+    }
+    t.fuel.resize(p.n_fuel);
+    for (uint64_t i = 0; i < p.n_fuel; ++i) {
+        if (p.fuel_indices[i] >= nc) { err = "fuel index out of range of the mesh"; return 1; }
+        t.fuel[i] = (uint32_t)p.fuel_indices[i];
+    }
+    t.cleft.assign(p.mesh.mesh_left, p.mesh.mesh_left + nc);
+    t.cdx.assign(p.mesh.delta_x, p.mesh.delta_x + nc);
+    t.cmat.assign(p.mesh.matid, p.mesh.matid + nc);
+    t.nsf64.resize(M * G);
+    for (uint64_t i = 0; i < M * G; ++i) t.nsf64[i] = (double)x.nut[i] * (double)x.sigf[i];
+    t.dx64.resize(nc);
+    for (uint64_t c = 0; c < nc; ++c) t.dx64[c] = (double)p.mesh.delta_x[c];
+    uint64_t inu = std::min<uint64_t>(M, M * G - 1);
+    t.conv_const = 3565e6 * 36.2 /
+        (200e6 * 1.602176634e-19 * (double)x.nut[inu] * (double)p.mesh.mesh_right[nc - 1]);
+    return 0;
+}

@@ -4,6 +4,7 @@
 #include <cstddef>
 #include <string>
 #include <vector>
+#include <cstdint>
 
 #include "../../include/nraps_gpu.h"
 
@@ -13,6 +14,26 @@ struct TableLayout {
     size_t total;
     double conv_const;
 };
+
+/* Tables of the event-based Woodcock engine for one problem instance (FP32).
+   Material regions are maximal runs of cells with the same matid and the same
+   (bitwise) width, so a cell index inside a region is arithmetic.
+     sigtr  = f32(sigt - mu*sigs) evaluated in FP64 (exact product)
+     pabs   = siga / sigtr,  nsf_st = (nut*sigf) / sigtr,  inv_st = 1 / sigtr
+     scdf   = transport-corrected scatter CDF (within-group term minus mu*sigs)
+     maj[g] = max of sigtr over the materials present, maj[G+g] = 1/maj[g]
+     grid   = first region of each of nbins equal bins of [0, L]             */
+struct EvHostTables {
+    uint32_t M = 0, G = 0, R = 0, nc = 0, nbins = 0, nfuel = 0;
+    float L = 0.f, inv_binw = 0.f, boundl = 0.f, boundr = 0.f;
+    std::vector<float> xs, scdf, chicdf, maj, rleft, rinvdx, cleft, cdx;
+    std::vector<uint8_t> rmat, cmat;
+    std::vector<uint32_t> rfirst, rncell, fuel;
+    std::vector<uint16_t> grid;
+    std::vector<double> nsf64, dx64;
+    double conv_const = 0.0;
+};
+int build_event_tables(const nraps_problem& p, EvHostTables& t, std::string& err);
 
 /* Returns 0 on success, else fills err. */
 template <class T>

@@ -359,6 +359,170 @@ static void run_generation(const Tab<T>& t, const nraps_opts& o, uint64_t gen, d
     out.kq += sk.kq;
 }
 
+
+/* ---- event-based Woodcock form (build-defined; no reference counterpart) --
+   Restates the FP32 delta-tracking history of the CUDA event kernel with the
+   shared software logarithm (the kernel's exact_log mode): tables, region
+   lookup, draw order and every rounding step are defined here independently
+   of the kernel source, from the same rules.                                */
+struct WTab {
+    uint32_t M, G, R, nc, nfuel;
+    float L, boundl, boundr;
+    std::vector<float> sigtr, pabs, nsf_st, inv_st, scdf, chicdf, maj, inv_maj;
+    std::vector<float> rleft, rinvdx, cleft, cdx;
+    std::vector<uint8_t> rmat, cmat;
+    std::vector<uint32_t> rfirst, rncell, fuel;
+};
+
+static WTab make_wtab(const nraps_problem& p) {
+    WTab t;
+    const nraps_xsdata& x = p.xsdata;
+    t.M = p.variables.mattypes; t.G = p.variables.energygroups; t.nc = (uint32_t)p.mesh.n_cells;
+    t.nfuel = (uint32_t)p.n_fuel; t.boundl = p.variables.boundl; t.boundr = p.variables.boundr;
+    uint32_t M = t.M, G = t.G;
+    t.sigtr.resize(M * G); t.pabs.resize(M * G); t.nsf_st.resize(M * G); t.inv_st.resize(M * G);
+    for (uint32_t m = 0; m < M; ++m)
+        for (uint32_t g = 0; g < G; ++g) {
+            uint32_t i = m + M * g, j = m * G + g;
+            float st = (float)((double)x.sigt[i] - (double)x.mu[i] * (double)x.sigs[i]);
+            t.sigtr[j] = st;
+            t.pabs[j] = x.siga[i] / st;
+            t.nsf_st[j] = (x.nut[i] * x.sigf[i]) / st;
+            t.inv_st[j] = 1.0f / st;
+        }
+    t.scdf.assign(M * G * G, 1.0f);
+    for (uint32_t m = 0; m < M; ++m)
+        for (uint32_t g = 0; g < G; ++g) {
+            uint32_t i = m + M * g;
+            float cum[64]; float c = 0.0f;
+            for (uint32_t e = 0; e < G; ++e) {
+                float s = x.scat_matrix[(uint64_t)G * G * m + (uint64_t)G * g + e];
+                if (e == g) s = s - x.mu[i] * x.sigs[i];
+                if (s < 0.0f) s = 0.0f;
+                c = c + s; cum[e] = c;
+            }
+            for (uint32_t e = 0; e < G; ++e) t.scdf[(m * G + g) * G + e] = c > 0.0f ? cum[e] / c : 1.0f;
+        }
+    t.chicdf.resize(M * G);
+    for (uint32_t m = 0; m < M; ++m) {
+        float c = 0.0f;
+        for (uint32_t g = 0; g < G; ++g) { c += x.chit[m + M * g]; t.chicdf[m * G + g] = c; }
+    }
+    std::vector<bool> present(M, false);
+    for (uint32_t c = 0; c < t.nc; ++c) {
+        uint8_t m = p.mesh.matid[c];
+        present[m] = true;
+        bool start = c == 0 || m != p.mesh.matid[c - 1] ||
+                     std::memcmp(&p.mesh.delta_x[c], &p.mesh.delta_x[c - 1], 4) != 0;
+        if (start) {
+            t.rleft.push_back(p.mesh.mesh_left[c]); t.rmat.push_back(m); t.rfirst.push_back(c);
+            t.rncell.push_back(1); t.rinvdx.push_back((float)(1.0 / (double)p.mesh.delta_x[c]));
+        } else {
+            t.rncell.back()++;
+        }
+    }
+    t.R = (uint32_t)t.rmat.size();
+    t.rleft.push_back(p.mesh.mesh_right[t.nc - 1]);
+    t.L = t.rleft[t.R];
+    t.maj.assign(G, 0.0f); t.inv_maj.assign(G, 0.0f);
+    for (uint32_t g = 0; g < G; ++g) {
+        float mj = 0.0f;
+        for (uint32_t m = 0; m < M; ++m) if (present[m]) mj = std::max(mj, t.sigtr[m * G + g]);
+        t.maj[g] = mj; t.inv_maj[g] = 1.0f / mj;
+    }
+    t.cleft.assign(p.mesh.mesh_left, p.mesh.mesh_left + t.nc);
+    t.cdx.assign(p.mesh.delta_x, p.mesh.delta_x + t.nc);
+    t.cmat.assign(p.mesh.matid, p.mesh.matid + t.nc);
+    for (uint64_t i = 0; i < p.n_fuel; ++i) t.fuel.push_back((uint32_t)p.fuel_indices[i]);
+    return t;
+}
+
+static float w_u24(Pcg32& r) { return (float)(r.next_u32() >> 8) * 0x1p-24f; }
+static float w_u24pos(Pcg32& r) { return (float)((r.next_u32() >> 8) + 1u) * 0x1p-24f; }
+static uint32_t w_chi(const float* cdf, uint32_t G, float v) {
+    size_t i = partition_point(G, [&](size_t j) { return cdf[j] < v; });
+    return (uint32_t)std::min<size_t>(i, G - 1);
+}
+/* region r with rleft[r] <= x < rleft[r+1] (the last region for x == L) */
+static uint32_t w_region(const WTab& t, float x) {
+    size_t r = std::upper_bound(t.rleft.begin(), t.rleft.begin() + t.R, x) - t.rleft.begin();
+    return r == 0 ? 0 : (uint32_t)(r - 1);
+}
+
+static void woodcock_history(const WTab& t, Pcg32& rng, double* tally, uint64_t& kq,
+                             nraps_history_record& rec, uint64_t max_events, bool bank, float inv_k,
+                             const nraps_site* src, uint32_t hid, std::vector<SiteU>* sites) {
+    const uint32_t G = t.G;
+    float x, mu; uint32_t g;
+    if (!src) {
+        uint32_t cell = t.fuel[((uint64_t)rng.next_u32() * t.nfuel) >> 32];
+        float sub = w_u24(rng);
+        x = t.cleft[cell] + sub * t.cdx[cell];
+        mu = 2.0f * w_u24(rng) - 1.0f;
+        g = w_chi(&t.chicdf[t.cmat[cell] * G], G, w_u24(rng));
+    } else {
+        x = src->x; g = src->group;
+        mu = 2.0f * w_u24(rng) - 1.0f;
+    }
+    uint64_t events = 0;
+    uint32_t seq = 0, last_cell = 0;
+    int fate = -1;
+    while (fate < 0) {
+        uint32_t r = 0, m = 0;
+        for (;;) {
+            if (++events > max_events) { fate = NRAPS_FATE_CAPPED; break; }
+            float d = -nr_logf(w_u24pos(rng)) * t.inv_maj[g];
+            x = x + mu * d;
+            int bounce = 0;
+            while (!(x >= 0.0f && x <= t.L)) {
+                if (x > t.L) {
+                    if (t.boundr > 0.0f) { x = t.L - (x - t.L); mu = -mu; }
+                    else { fate = NRAPS_FATE_LEAKED; break; }
+                } else {
+                    if (t.boundl > 0.0f) { x = -x; mu = -mu; }
+                    else { fate = NRAPS_FATE_LEAKED; break; }
+                }
+                if (++bounce > 1000) { fate = NRAPS_FATE_CAPPED; break; }
+            }
+            if (fate >= 0) break;
+            r = w_region(t, x);
+            m = t.rmat[r];
+            if (w_u24(rng) * t.maj[g] < t.sigtr[m * G + g]) break;
+            rec.crossings++;
+        }
+        if (fate >= 0) break;
+        uint32_t j = m * G + g;
+        float rel = (x - t.rleft[r]) * t.rinvdx[r];
+        uint32_t k = rel > 0.0f ? (uint32_t)rel : 0u;
+        if (k >= t.rncell[r]) k = t.rncell[r] - 1;
+        uint32_t cell = t.rfirst[r] + k;
+        last_cell = cell;
+        tally[(uint64_t)g * t.nc + cell] += (double)t.inv_st[j];
+        kq += nr_fix((double)t.nsf_st[j]);
+        rec.collisions++;
+        rec.track += (double)t.inv_st[j];
+        rec.nsf_track += (double)t.nsf_st[j];
+        if (bank) {
+            float nu = t.nsf_st[j] * inv_k + w_u24(rng);
+            int n = (int)std::floor(nu);
+            if (n > 64) n = 64;
+            for (int i = 0; i < n; ++i) {
+                uint32_t sg = w_chi(&t.chicdf[m * G], G, w_u24(rng));
+                if (sites) sites->push_back(SiteU{x, cell, sg, hid, seq});
+                ++seq;
+            }
+        }
+        if (w_u24(rng) < t.pabs[j]) { fate = NRAPS_FATE_ABSORBED; break; }
+        float xi = w_u24(rng);
+        uint32_t ng = G - 1;
+        for (uint32_t e = 0; e + 1 < G; ++e) if (xi < t.scdf[j * G + e]) { ng = e; break; }
+        g = ng;
+        mu = 2.0f * w_u24(rng) - 1.0f;
+    }
+    rec.fate = fate; rec.final_group = g; rec.final_x = (double)x; rec.final_cell = last_cell;
+    rec.n_sites = seq; rec.draws = rng.draws;
+}
+
 } // namespace orc
 
 using namespace orc;
@@ -598,6 +762,40 @@ int oracle_monte_carlo(const nraps_problem* p, const nraps_opts* o, uint32_t thr
         return acc64 ? mc_impl<float, double>(p, o, threads, max_generations, res)
                      : mc_impl<float, float>(p, o, threads, max_generations, res);
     return mc_impl<double, double>(p, o, threads, max_generations, res);
+}
+
+/* One event-form generation, histories in id order (exact_log semantics). */
+int oracle_trace_woodcock(const nraps_problem* p, const nraps_opts* o, uint64_t gen, double k,
+                          const nraps_site* sites_in, uint64_t n_in,
+                          nraps_history_record* records, uint64_t n_records, double* tally,
+                          nraps_site* sites_out, uint64_t cap_out, uint64_t* n_out, uint64_t* kq_out) {
+    uint64_t N = p->variables.histories;
+    if (n_records != N) return NRAPS_ERR_INVALID;
+    WTab t = make_wtab(*p);
+    uint64_t seed = gen_seed(o->seed, gen);
+    uint64_t maxev = o->max_events ? o->max_events : (1ULL << 24);
+    bool bank = o->mode == NRAPS_MODE_BANK;
+    float inv_k = (float)(1.0 / k);
+    std::vector<double> tl((uint64_t)t.G * t.nc, 0.0);
+    std::vector<SiteU> sites;
+    uint64_t kq = 0;
+    for (uint64_t h = 0; h < N; ++h) {
+        Pcg32 rng(seed, h);
+        nraps_history_record r; std::memset(&r, 0, sizeof r);
+        const nraps_site* src = nullptr;
+        if (bank && sites_in && n_in) src = &sites_in[(h * n_in) / N];
+        woodcock_history(t, rng, tl.data(), kq, r, maxev, bank, inv_k, src, (uint32_t)h, bank ? &sites : nullptr);
+        records[h] = r;
+    }
+    if (tally) std::memcpy(tally, tl.data(), tl.size() * 8);
+    if (kq_out) *kq_out = kq;
+    if (n_out) *n_out = sites.size();
+    if (sites_out) {
+        uint64_t n = std::min<uint64_t>(cap_out, sites.size());
+        for (uint64_t i = 0; i < n; ++i) sites_out[i] = nraps_site{sites[i].x, sites[i].cell, sites[i].group, 0};
+        if (sites.size() > cap_out) return NRAPS_ERR_CAPACITY;
+    }
+    return NRAPS_OK;
 }
 
 unsigned oracle_hardware_threads(void) { return std::thread::hardware_concurrency(); }

@@ -47,6 +47,7 @@ def lib():
         L.oracle_monte_carlo.argtypes = [C.POINTER(abi.Problem), C.POINTER(abi.Opts), C.c_uint32,
                                          C.c_int, C.c_uint64, C.POINTER(abi.Result)]
         L.oracle_hardware_threads.restype = C.c_uint
+        L.oracle_trace_woodcock.argtypes = L.oracle_trace_generation.argtypes
         _lib = L
     return _lib
 
@@ -149,3 +150,26 @@ def monte_carlo(prob: abi.ProblemArrays, opts: abi.Opts, threads: int = 1, acc64
 
 def hardware_threads() -> int:
     return int(lib().oracle_hardware_threads())
+
+
+def trace_woodcock(prob: abi.ProblemArrays, opts: abi.Opts, gen: int, k: float, sites_in=None, site_cap=None):
+    """One event-form (Woodcock, exact_log) generation: (records, tally, sites, kq)."""
+    N = prob.histories
+    rec = np.zeros(N, abi.RECORD_DTYPE)
+    tally = np.zeros(prob.energygroups * prob.n_cells, np.float64)
+    cap = site_cap if site_cap is not None else 4 * prob.histories + 64
+    sites = np.zeros(cap, abi.SITE_DTYPE)
+    n_out = C.c_uint64()
+    kq = C.c_uint64()
+    pv = prob.view()
+    sin, n_in = None, 0
+    if sites_in is not None and len(sites_in):
+        sites_in = np.ascontiguousarray(sites_in, abi.SITE_DTYPE)
+        sin, n_in = sites_in.ctypes.data_as(C.c_void_p), len(sites_in)
+    st = lib().oracle_trace_woodcock(
+        C.byref(pv), C.byref(opts), gen, k, sin, n_in, rec.ctypes.data_as(C.c_void_p), N,
+        tally.ctypes.data_as(C.POINTER(C.c_double)), sites.ctypes.data_as(C.c_void_p), cap,
+        C.byref(n_out), C.byref(kq))
+    if st != 0:
+        raise RuntimeError(f"oracle_trace_woodcock failed: {st}")
+    return rec, tally, sites[: n_out.value].copy(), int(kq.value)

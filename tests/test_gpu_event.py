@@ -1,0 +1,133 @@
+"""Event-based Woodcock engine through the C ABI.
+
+exact_log mode: every per-history record, the fixed-point k score and the
+ordered fission bank equal the CPU restatement of the Woodcock history bit for
+bit, for several (events per pass, passes, block size) shapes of the queue
+machinery.  Fast mode (hardware log): results do not depend on the shape, and
+agree statistically with the plain FP64 kernel (k within 3 sigma, flux chi^2
+per group on independent generations).
+"""
+import numpy as np
+import pytest
+from scipy import stats as sps
+
+from nraps_gb300 import abi, api, synth
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+SHAPES = [dict(events_per_pass=1, passes=4, block_size=128),
+          dict(events_per_pass=4, passes=2, block_size=256),
+          dict(events_per_pass=16, passes=1, block_size=512)]
+
+
+def small(hist=3000, gens=12, skip=4, seed=3):
+    return synth.plain_small(seed).with_(histories=hist, generations=gens, skip=skip)
+
+
+def _records_equal(g, w):
+    for f in ("collisions", "crossings", "fate", "final_cell", "final_group", "n_sites", "draws"):
+        bad = np.nonzero(g[f] != w[f])[0]
+        assert bad.size == 0, (f, bad[:5], g[f][bad[:5]], w[f][bad[:5]])
+    for f in ("final_x", "track", "nsf_track"):
+        bad = np.nonzero(g[f].view(np.int64) != w[f].view(np.int64))[0]
+        assert bad.size == 0, (f, bad[:5], g[f][bad[:5]], w[f][bad[:5]])
+
+
+@pytest.mark.parametrize("shape", SHAPES, ids=["K1P4b128", "K4P2b256", "K16P1b512"])
+@pytest.mark.parametrize("mode", [abi.MODE_PHYSICS, abi.MODE_BANK])
+def test_event_trace_bitexact(ctx_factory, mode, shape):
+    p = small()
+    opts = dict(seed=41, mode=mode, precision=abi.PREC_FP32, tracking=abi.TRACK_WOODCOCK, exact_log=1, **shape)
+    o = abi.make_opts(**opts)
+    ctx = ctx_factory(**opts)
+    sites_in = None
+    gen = 2
+    if mode == abi.MODE_BANK:
+        _, _, sites_in, _ = O.trace_woodcock(p, o, 0, 1.0)
+        gen = 1
+    grec, gt, gs, gkq = ctx.trace(p, gen, 0.95, sites_in=sites_in)
+    wrec, wt, ws, wkq = O.trace_woodcock(p, o, gen, 0.95, sites_in=sites_in)
+    _records_equal(grec, wrec)
+    assert gkq == wkq
+    np.testing.assert_allclose(gt, wt, rtol=1e-12, atol=0)
+    if mode == abi.MODE_BANK:
+        assert len(gs) == len(ws) and np.array_equal(gs, ws)
+
+
+def test_event_reflective_bitexact(ctx_factory):
+    import os
+    from .conftest import GOLDEN
+    inp = api.process_input(os.path.join(GOLDEN, "inputs", "TestCaseC.txt"))
+    mesh, fuel = api.mesh_gen(inp.matid, inp.variables, inp.delta_x)
+    p = api.problem_from_input(inp, mesh, fuel).with_(histories=2000, generations=3, skip=1)
+    opts = dict(seed=5, mode=abi.MODE_PHYSICS, precision=abi.PREC_FP32, tracking=abi.TRACK_WOODCOCK, exact_log=1)
+    grec, gt, _, gkq = ctx_factory(**opts).trace(p, 0, 1.0)
+    wrec, wt, _, wkq = O.trace_woodcock(p, abi.make_opts(**opts), 0, 1.0)
+    _records_equal(grec, wrec)
+    assert gkq == wkq and np.all(grec["fate"] != abi.FATE_LEAKED)
+
+
+def test_event_results_independent_of_queue_shape(ctx_factory):
+    p = small(hist=20000, gens=10, skip=3)
+    ks = []
+    for shape in SHAPES:
+        r = ctx_factory(seed=7, mode=abi.MODE_BANK, precision=abi.PREC_FP32,
+                        tracking=abi.TRACK_WOODCOCK, **shape).solve(p)
+        ks.append(r.k64)
+    assert np.array_equal(ks[0], ks[1]) and np.array_equal(ks[0], ks[2])
+
+
+def test_event_graph_replay_equals_direct(ctx_factory):
+    p = small(hist=20000, gens=10, skip=3)
+    base = dict(seed=9, mode=abi.MODE_BANK, precision=abi.PREC_FP32, tracking=abi.TRACK_WOODCOCK)
+    a = ctx_factory(use_graphs=1, **base).solve(p)
+    b = ctx_factory(use_graphs=0, **base).solve(p)
+    assert np.array_equal(a.k64, b.k64)
+
+
+def test_event_k_agrees_with_plain_fp64_bank(ctx_factory):
+    # same seeds, same physics, different tracking and precision
+    p = small(hist=40000, gens=60, skip=20)
+    ev = ctx_factory(seed=11, mode=abi.MODE_BANK, precision=abi.PREC_FP32, tracking=abi.TRACK_WOODCOCK).solve(p)
+    pl = ctx_factory(seed=11, mode=abi.MODE_BANK, precision=abi.PREC_FP64).solve(p)
+    d = abs(ev.stats.k_mean - pl.stats.k_mean)
+    # generations of a power iteration are correlated: inflate sigma by 2
+    sig = 2.0 * np.hypot(ev.stats.k_sigma, pl.stats.k_sigma)
+    assert d < 3 * sig, (ev.stats.k_mean, pl.stats.k_mean, sig)
+    assert ev.stats.virtual_collisions > 0 and ev.stats.crossings == 0
+
+
+def test_event_flux_chi2_against_plain_fp64(ctx_factory):
+    # PHYSICS mode: every generation restarts from the fresh source, so
+    # generations are independent and the per-bin standard errors are valid
+    p = small(hist=40000, gens=40, skip=2)
+    ev = ctx_factory(seed=13, mode=abi.MODE_PHYSICS, precision=abi.PREC_FP32, tracking=abi.TRACK_WOODCOCK).solve(p)
+    pl = ctx_factory(seed=13, mode=abi.MODE_PHYSICS, precision=abi.PREC_FP64).solve(p)
+    G, nc = p.energygroups, p.n_cells
+    m1, s1 = ev.flux_mean.reshape(G, nc), ev.flux_sem.reshape(G, nc)
+    m2, s2 = pl.flux_mean.reshape(G, nc), pl.flux_sem.reshape(G, nc)
+    for g in range(G):
+        ok = (s1[g] > 0) & (s2[g] > 0)
+        chi2 = float((((m1[g] - m2[g]) ** 2) / (s1[g] ** 2 + s2[g] ** 2))[ok].sum())
+        dof = int(ok.sum())
+        pval = sps.chi2.sf(chi2, dof)
+        assert pval > 1e-4, (g, chi2, dof, pval)
+    assert abs(ev.stats.k_mean - pl.stats.k_mean) < 3 * np.hypot(ev.stats.k_sigma, pl.stats.k_sigma)
+
+
+def test_event_fast_log_matches_exact_log(ctx_factory):
+    p = small(hist=20000, gens=10, skip=3)
+    base = dict(seed=17, mode=abi.MODE_BANK, precision=abi.PREC_FP32, tracking=abi.TRACK_WOODCOCK)
+    fast = ctx_factory(exact_log=0, **base).solve(p)
+    exact = ctx_factory(exact_log=1, **base).solve(p)
+    assert abs(fast.stats.k_mean - exact.stats.k_mean) < 3 * 2 * np.hypot(fast.stats.k_sigma, exact.stats.k_sigma)
+
+
+def test_event_bank_overflow_is_reported(ctx_factory):
+    p = small(hist=5000, gens=4, skip=1)
+    ctx = ctx_factory(seed=3, mode=abi.MODE_BANK, precision=abi.PREC_FP32, tracking=abi.TRACK_WOODCOCK,
+                      bank_factor=0.01)
+    with pytest.raises(api.NrapsError) as e:
+        ctx.solve(p)
+    assert e.value.status == abi.ERR_CAPACITY

@@ -102,9 +102,11 @@ def test_compat_solve_matches_reference_f32_arithmetic(ctx_factory):
     g = ctx_factory(**opts).solve(p)
     w64 = O.monte_carlo(p, abi.make_opts(**opts), threads=7, acc64=True)
     w32 = O.monte_carlo(p, abi.make_opts(**opts), threads=7, acc64=False)
-    np.testing.assert_allclose(g.k, w64.k, rtol=1e-6)
+    # the oracle finalizes in f32 as the reference does (k summed over 2000
+    # bins in f32): 2e-5 relative; the GPU sums in FP64
+    np.testing.assert_allclose(g.k, w64.k, rtol=2e-5)
     np.testing.assert_allclose(g.k, w32.k, rtol=1e-3)
-    np.testing.assert_allclose(g.k_fund[2:], w64.k_fund[2:], rtol=1e-6)
+    np.testing.assert_allclose(g.k_fund[2:], w64.k_fund[2:], rtol=2e-5)
     np.testing.assert_allclose(g.flux, w64.flux, rtol=1e-5)
     np.testing.assert_allclose(g.assembly_average, w64.assembly_average, rtol=1e-5)
 
