@@ -143,6 +143,7 @@ def measure_device(prob, arm: str, steps: int, warmup: int, seed: int, device: i
     ext = torch.cuda.ExternalStream(ctx.stream_ptr, device=device)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{device}")
     s.run(warmup)
+    tuning = s.tuning() if arm == "event" else None
     t0 = s.timing()
     launches0 = ctx.launches
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
@@ -161,7 +162,8 @@ def measure_device(prob, arm: str, steps: int, warmup: int, seed: int, device: i
     out = dict(ms=ms, histories=steps * prob.histories, collisions=t1["collisions"] - t0["collisions"],
                transport_ms=t1["transport_ms"] - t0["transport_ms"],
                transport_launches=t1["transport_launches"] - t0["transport_launches"],
-               launches=ctx.launches - launches0 - 0, k_mean=res.stats.k_mean, k_sigma=res.stats.k_sigma)
+               launches=ctx.launches - launches0, k_mean=res.stats.k_mean, k_sigma=res.stats.k_sigma,
+               tuning=tuning)
     # the flush zero_() launches are torch's, not ours; ctx.launches counts ours
     s.close()
     ctx.close()
@@ -353,7 +355,7 @@ def main():
                        "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
             "sigma_k_pcm": d["k_sigma"] * 1e5, "k_mean": d["k_mean"],
             "collisions_per_s": world * d["collisions"] / (ms / 1000.0),
-            "gpu_launches": d["launches"],
+            "gpu_launches": d["launches"], "launch_shape": d["tuning"],
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "plain": plain, "clocks": clk,
         }
         print(json.dumps(line), flush=True)

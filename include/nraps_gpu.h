@@ -232,6 +232,13 @@ int  nraps_session_set_profile(nraps_session* s, int on);
 int  nraps_session_timing(nraps_session* s, double* transport_ms, double* total_ms,
                           uint64_t* transport_launches, uint64_t* collisions,
                           uint64_t* histories);
+/* WOODCOCK sessions: the launch shape in use.  With block_size,
+   events_per_pass and passes all 0 in the options, the first inactive
+   generations each try one candidate shape (synchronously) and the fastest
+   is kept; results do not depend on the shape.  tried_ms receives the
+   transport time of each candidate tried (up to tried_cap). */
+int  nraps_session_tuning(nraps_session* s, uint32_t* block, uint32_t* events_per_pass,
+                          uint32_t* passes, uint32_t* n_tried, float* tried_ms, uint32_t tried_cap);
 /* generations completed so far (enqueued work included after sync) */
 uint64_t nraps_session_generation(const nraps_session* s);
 void nraps_session_destroy(nraps_session* s);

@@ -121,6 +121,11 @@ struct nraps_session {
     std::vector<cudaEvent_t> gev;      /* pairs around whole generations        */
     double transport_ms = 0.0, total_ms = 0.0;
     uint64_t transport_launches = 0;
+    /* autotuning of the event engine over the inactive generations */
+    std::vector<EvParams> tune_cand;
+    std::vector<float> tune_ms;
+    size_t tune_next = 0;
+    bool tuned = false;
     ~nraps_session() {
         if (gexec) cudaGraphExecDestroy(gexec);
         for (cudaEvent_t e : tev) cudaEventDestroy(e);
@@ -192,8 +197,9 @@ int create_session(nraps_ctx* ctx, const nraps_problem* p, bool with_records, nr
             CK(cudaMemsetAsync(s->scount.p, 0, s->n_hist * 4, sm));
         }
         CK(s->bank0.alloc(s->cap * sizeof(nraps_site))); CK(s->bank1.alloc(s->cap * sizeof(nraps_site)));
-        CK(s->hist.alloc(s->nc * 4));
-        CK(cudaMemsetAsync(s->hist.p, 0, s->nc * 4, sm));
+        uint64_t hist_words = s->nc * (woodcock ? EV_HIST_STRIDE : 1);
+        CK(s->hist.alloc(hist_words * 4));
+        CK(cudaMemsetAsync(s->hist.p, 0, hist_words * 4, sm));
     }
     if (with_records) {
         CK(s->records.alloc(s->n_hist * sizeof(nraps_history_record)));
@@ -265,6 +271,21 @@ int create_session(nraps_ctx* ctx, const nraps_problem* p, bool with_records, nr
         if (with_records) s->ev->set_records(s->records.as<nraps_history_record>());
         est = s->ev->commit(sm, e2);
         if (est) return set_err(ctx, est, e2);
+        /* tune block size, collisions per pass and pass count unless all given */
+        if (!with_records && s->o.block_size == 0 && s->o.events_per_pass == 0 && s->o.passes == 0) {
+            const uint32_t cand[][3] = {{256, 4, 3}, {256, 1, 8}, {256, 2, 4}, {256, 8, 2}, {256, 16, 1},
+                                        {256, 4, 1}, {128, 4, 3}, {128, 8, 2}, {128, 2, 4}, {256, 2, 2}};
+            size_t n = sizeof(cand) / sizeof(cand[0]);
+            size_t budget = (size_t)std::min<uint64_t>(s->v.skip, n);
+            for (size_t i = 0; i < budget; ++i) {
+                EvParams pr;
+                pr.block = cand[i][0]; pr.K = cand[i][1]; pr.passes = cand[i][2];
+                s->tune_cand.push_back(pr);
+            }
+            s->tuned = s->tune_cand.size() < 2;
+        } else {
+            s->tuned = true;
+        }
     }
     s->cell_dx_host.assign(p->mesh.delta_x, p->mesh.delta_x + s->nc);
     CK(cudaStreamSynchronize(sm));
@@ -412,6 +433,34 @@ int nraps_session_run(nraps_session* s, uint64_t n) {
     cudaStream_t sm = ctx->stream;
     if (s->enqueued + n > s->gens) n = s->gens - s->enqueued;
     for (uint64_t i = 0; i < n; ++i) {
+        if (s->ev && !s->tuned) {
+            /* one candidate per generation: histories do not depend on the
+               candidate, so tuning leaves every result unchanged */
+            EvParams& pr = s->tune_cand[s->tune_next];
+            s->ev->params = pr;
+            s->ev->size_grid();
+            cudaEvent_t e0, e1;
+            CK(cudaEventCreate(&e0)); CK(cudaEventCreate(&e1));
+            int r = s->ev->enqueue_generation(sm, true, e0, e1);
+            if (r < 0) return set_err(ctx, NRAPS_ERR_CUDA, std::string("kernel launch failed: ") + cudaGetErrorString(cudaGetLastError()));
+            ctx->launches += (uint64_t)r;
+            s->transport_launches += s->ev->launches_per_generation();
+            CK(cudaEventSynchronize(e1));
+            float ms = 0.f;
+            CK(cudaEventElapsedTime(&ms, e0, e1));
+            cudaEventDestroy(e0); cudaEventDestroy(e1);
+            s->tune_ms.push_back(ms);
+            s->transport_ms += ms;
+            if (++s->tune_next == s->tune_cand.size()) {
+                size_t best = 0;
+                for (size_t j = 1; j < s->tune_ms.size(); ++j) if (s->tune_ms[j] < s->tune_ms[best]) best = j;
+                s->ev->params = s->tune_cand[best];
+                s->ev->size_grid();
+                s->tuned = true;
+            }
+            s->enqueued++;
+            continue;
+        }
         if (s->profile) {
             cudaEvent_t e[4];
             for (int j = 0; j < 4; ++j) CK(cudaEventCreate(&e[j]));
@@ -473,6 +522,18 @@ int nraps_session_sync(nraps_session* s) {
     int st = read_state(s, g);
     if (st) return st;
     return state_status(s, g);
+}
+
+int nraps_session_tuning(nraps_session* s, uint32_t* block, uint32_t* events_per_pass, uint32_t* passes,
+                         uint32_t* n_tried, float* tried_ms, uint32_t tried_cap) {
+    if (!s) return NRAPS_ERR_INVALID;
+    if (!s->ev) return set_err(s->ctx, NRAPS_ERR_INVALID, "tuning applies to WOODCOCK sessions");
+    if (block) *block = s->ev->params.block;
+    if (events_per_pass) *events_per_pass = s->ev->params.K;
+    if (passes) *passes = s->ev->params.passes;
+    if (n_tried) *n_tried = (uint32_t)s->tune_ms.size();
+    for (uint32_t i = 0; tried_ms && i < tried_cap && i < s->tune_ms.size(); ++i) tried_ms[i] = s->tune_ms[i];
+    return NRAPS_OK;
 }
 
 int nraps_session_timing(nraps_session* s, double* transport_ms, double* total_ms,

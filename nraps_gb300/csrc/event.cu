@@ -30,6 +30,9 @@ namespace {
 
 constexpr uint32_t NSLAB = 128;
 constexpr uint32_t MAX_PASSES = 16;
+/* one entropy counter per 128-byte line: the fuel cells' site counts then
+   spread over every L2 slice instead of a few dozen lines */
+constexpr uint32_t HIST_STRIDE = 32;
 
 struct EvInst {
     const float* xs;        /* [(m*G+g)*4]: sigtr, pabs, nsf_st, inv_st        */
@@ -72,7 +75,9 @@ struct EvArgs {
     unsigned long long* qrng[2];
     uint32_t* qid[2];
     uint32_t* qpk[2];
-    unsigned long long* qcount;   /* MAX_PASSES+2                             */
+    unsigned long long* qcount;   /* MAX_PASSES+2: particles queued by pass p */
+    unsigned long long* claim;    /* MAX_PASSES+2: input claimed by pass p    */
+    unsigned long long* blocks_done; /* finalize: blocks that finished          */
     float* sx;
     uint32_t* scell;
     uint32_t* sgi;                /* group | inst << 4                        */
@@ -144,67 +149,64 @@ struct Acc {
     uint32_t coll, virt, absorbed, leaked, capped;
 };
 
-/* Run one particle for up to K real collisions.  Returns true if alive. */
+/* One flight to the next real collision and that collision.
+   Returns 0 while the particle lives, else its NRAPS_FATE_* + 1. */
 template <bool EXACT, bool BANK, bool REC>
-__device__ bool run_particle(const EvArgs& a, const EvInst& I, const TView& t, Part& p, uint32_t K,
-                             float inv_k, Acc& acc, unsigned long long& kq_part) {
+__device__ __forceinline__ int step_particle(const EvArgs& a, const EvInst& I, const TView& t, Part& p,
+                                             float inv_k, Acc& acc, uint64_t& events,
+                                             unsigned long long& kq_part) {
     const uint32_t G = t.G;
-    uint64_t events = 0;
     uint32_t draws = 0;
     auto next = [&]() -> uint32_t { if (REC) ++draws; return nr_pcg32_next(&p.rng); };
     nraps_history_record* rec = (REC && p.inst == 0) ? &a.rec[p.local] : nullptr;
     int fate = -1;
-    for (uint32_t c = 0; c < K && fate < 0; ++c) {
-        uint32_t r = 0, m = 0;
-        /* flight to the next real collision */
-        for (;;) {
-            if (++events > a.max_events) { fate = NRAPS_FATE_CAPPED; break; }
-            float d = __fmul_rn(neg_log<EXACT>(u24pos(next())), t.maj[G + p.g]);
-            p.x = __fadd_rn(p.x, __fmul_rn(p.mu, d));
-            int bounce = 0;
-            while (!(p.x >= 0.0f && p.x <= t.L)) {
-                if (p.x > t.L) {
-                    if (t.boundr > 0.0f) { p.x = __fsub_rn(t.L, __fsub_rn(p.x, t.L)); p.mu = -p.mu; }
-                    else { fate = NRAPS_FATE_LEAKED; break; }
-                } else {
-                    if (t.boundl > 0.0f) { p.x = -p.x; p.mu = -p.mu; }
-                    else { fate = NRAPS_FATE_LEAKED; break; }
-                }
-                if (++bounce > 1000) { fate = NRAPS_FATE_CAPPED; break; }
+    uint32_t r = 0, m = 0;
+    for (;;) {
+        if (++events > a.max_events) { fate = NRAPS_FATE_CAPPED; break; }
+        float d = __fmul_rn(neg_log<EXACT>(u24pos(next())), t.maj[G + p.g]);
+        p.x = __fadd_rn(p.x, __fmul_rn(p.mu, d));
+        int bounce = 0;
+        while (!(p.x >= 0.0f && p.x <= t.L)) {
+            if (p.x > t.L) {
+                if (t.boundr > 0.0f) { p.x = __fsub_rn(t.L, __fsub_rn(p.x, t.L)); p.mu = -p.mu; }
+                else { fate = NRAPS_FATE_LEAKED; break; }
+            } else {
+                if (t.boundl > 0.0f) { p.x = -p.x; p.mu = -p.mu; }
+                else { fate = NRAPS_FATE_LEAKED; break; }
             }
-            if (fate >= 0) break;
-            r = region_of(t, p.x);
-            m = t.rmat[r];
-            float s = t.xs[(m * G + p.g) * 4];
-            if (__fmul_rn(u24(next()), t.maj[p.g]) < s) break;
-            acc.virt++;
-            if (REC && rec) rec->crossings++;
+            if (++bounce > 1000) { fate = NRAPS_FATE_CAPPED; break; }
         }
         if (fate >= 0) break;
+        r = region_of(t, p.x);
+        m = t.rmat[r];
+        if (__fmul_rn(u24(next()), t.maj[p.g]) < t.xs[(m * G + p.g) * 4]) break;
+        acc.virt++;
+        if (REC && rec) rec->crossings++;
+    }
+    if (fate < 0) {
         /* real collision */
         acc.coll++;
-        const float* X = &t.xs[(m * G + p.g) * 4];
+        const float4 X = *reinterpret_cast<const float4*>(&t.xs[(m * G + p.g) * 4]);
         float rel = __fmul_rn(__fsub_rn(p.x, t.left[r]), t.invdx[r]);
         uint32_t nr = t.ncell[r];
         uint32_t k = rel > 0.0f ? (uint32_t)rel : 0u;
         if (k >= nr) k = nr - 1;
         uint32_t cell = t.first[r] + k;
-        float inv_st = X[3], nsf_st = X[2];
-        atomicAdd(&I.tally[(uint64_t)p.g * I.nc + cell], (double)inv_st);
-        unsigned long long q = nr_fix((double)nsf_st);
+        atomicAdd(&I.tally[(uint64_t)p.g * I.nc + cell], (double)X.w);
+        unsigned long long q = nr_fix((double)X.z);
         acc.kq += q;
         kq_part += q;
         if (REC && rec) {
-            rec->collisions++; rec->track += (double)inv_st; rec->nsf_track += (double)nsf_st;
+            rec->collisions++; rec->track += (double)X.w; rec->nsf_track += (double)X.z;
             rec->final_cell = cell;
         }
         if (BANK) {
-            float nu = __fadd_rn(__fmul_rn(nsf_st, inv_k), u24(next()));
+            float nu = __fadd_rn(__fmul_rn(X.z, inv_k), u24(next()));
             int n = (int)floorf(nu);
             if (n > 64) n = 64;
             for (int i = 0; i < n; ++i) {
                 uint32_t sg = chi_group(t.chi + m * G, G, u24(next()));
-                uint32_t slab = blockIdx.x % NSLAB;
+                uint32_t slab = (blockIdx.x * 8 + (threadIdx.x >> 5)) % NSLAB;
                 unsigned long long j = nrdev::agg_inc(&a.slab_count[slab]);
                 if (j < a.slab_cap && p.seq < 0xFFFFu) {
                     uint64_t at = (uint64_t)slab * a.slab_cap + j;
@@ -219,16 +221,19 @@ __device__ bool run_particle(const EvArgs& a, const EvInst& I, const TView& t, P
                 p.seq++;
             }
         }
-        if (u24(next()) < X[1]) { fate = NRAPS_FATE_ABSORBED; break; }
-        float xi = u24(next());
-        const float* cdf = t.scdf + (m * G + p.g) * G;
-        uint32_t ng = G - 1;
-        for (uint32_t e = 0; e + 1 < G; ++e) if (xi < cdf[e]) { ng = e; break; }
-        p.g = ng;
-        p.mu = __fsub_rn(__fmul_rn(2.0f, u24(next())), 1.0f);
+        if (u24(next()) < X.y) {
+            fate = NRAPS_FATE_ABSORBED;
+        } else {
+            float xi = u24(next());
+            const float* cdf = t.scdf + (m * G + p.g) * G;
+            uint32_t ng = G - 1;
+            for (uint32_t e = 0; e + 1 < G; ++e) if (xi < cdf[e]) { ng = e; break; }
+            p.g = ng;
+            p.mu = __fsub_rn(__fmul_rn(2.0f, u24(next())), 1.0f);
+        }
     }
     if (REC && rec) rec->draws += draws;
-    if (fate < 0) return true;
+    if (fate < 0) return 0;
     if (fate == NRAPS_FATE_ABSORBED) acc.absorbed++;
     else if (fate == NRAPS_FATE_LEAKED) acc.leaked++;
     else { acc.capped++; atomicOr(&I.st->error, NR_ERR_CAPPED); }
@@ -237,7 +242,7 @@ __device__ bool run_particle(const EvArgs& a, const EvInst& I, const TView& t, P
         rec->fate = fate; rec->final_group = p.g; rec->final_x = (double)p.x;
         rec->n_sites = p.seq;
     }
-    return false;
+    return fate + 1;
 }
 
 __device__ __forceinline__ TView global_view(const EvInst& I) {
@@ -256,11 +261,44 @@ __host__ __device__ __forceinline__ size_t smem_words(uint32_t M, uint32_t G, ui
     return (bytes + 15) / 16 * 16;
 }
 
+constexpr int WARPS_MAX = 8;        /* blocks of at most 256 threads          */
+constexpr uint32_t CHUNK = 64;      /* particles a warp claims per atomic     */
+constexpr uint32_t STAGE = 64;      /* survivors a warp stages before a flush */
+
+struct Stage {
+    float x[STAGE], mu[STAGE];
+    unsigned long long rng[STAGE];
+    uint32_t id[STAGE], pk[STAGE];
+};
+
+/* flush the first `n` staged survivors of warp w to the out queue (warp-wide) */
+__device__ __forceinline__ void flush_stage(const EvArgs& a, Stage& sg, uint32_t n, int pass, int qout,
+                                            uint32_t lane) {
+    unsigned long long base = 0;
+    if (lane == 0) base = atomicAdd(&a.qcount[pass], (unsigned long long)n);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    for (uint32_t i = lane; i < n; i += 32) {
+        uint64_t o = base + i;
+        a.qx[qout][o] = sg.x[i];
+        a.qmu[qout][o] = sg.mu[i];
+        a.qrng[qout][o] = sg.rng[i];
+        a.qid[qout][o] = sg.id[i];
+        a.qpk[qout][o] = sg.pk[i];
+    }
+}
+
+/*
+ * One queue pass.  Each warp works on its own: it claims input particles 64
+ * at a time (one global atomic), hands them to idle lanes, advances every
+ * live particle by one real collision per iteration, and stages particles
+ * that completed K collisions in shared memory, flushing 32 at a time to the
+ * output queue with one atomic.  Lanes whose particle dies take the next
+ * input particle, so the warp stays full until the input runs out.
+ */
 template <bool SOURCE, bool ONE, bool EXACT, bool BANK, bool REC>
-__global__ void __launch_bounds__(512) ev_pass(EvArgs a, int pass, uint32_t K) {
+__global__ void __launch_bounds__(256, 3) ev_pass(EvArgs a, int pass, uint32_t K) {
     extern __shared__ __align__(16) unsigned char smem[];
-    __shared__ uint32_t s_scan[33];
-    __shared__ unsigned long long s_base;
+    __shared__ Stage s_stage[WARPS_MAX];
     TView t;
     if (ONE) {
         const EvInst& I = a.inst[0];
@@ -292,91 +330,149 @@ __global__ void __launch_bounds__(512) ev_pass(EvArgs a, int pass, uint32_t K) {
         t.G = G; t.R = R; t.nbins = NB; t.L = I.L; t.inv_binw = I.inv_binw;
         t.boundl = I.boundl; t.boundr = I.boundr;
     }
+    const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const unsigned lt = (1u << lane) - 1u;
+    Stage& sg = s_stage[w];
     const int qin = (pass - 1) & 1, qout = pass & 1;
     const uint64_t n_in = SOURCE ? a.n_total : a.qcount[pass - 1];
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    const uint64_t trips = (n_in + stride - 1) / stride;
+    unsigned long long* claim = &a.claim[pass];
+    uint64_t pool_next = 0, pool_end = 0;     /* warp-uniform claimed range */
+    bool exhausted = false;
+    uint32_t staged = 0;                      /* warp-uniform               */
     Acc acc = {0, 0, 0, 0, 0, 0};
-    for (uint64_t tr = 0; tr < trips; ++tr) {
-        uint64_t idx = tr * stride + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-        bool alive = false;
-        Part p;
-        if (idx < n_in) {
-            if (SOURCE) {
-                uint32_t inst = 0;
-                if (!ONE) {
-                    uint32_t lo = 0, hi = a.n_inst;        /* last begin <= idx */
-                    while (hi - lo > 1) {
-                        uint32_t mid = (lo + hi) >> 1;
-                        if (a.inst_begin[mid] <= idx) lo = mid; else hi = mid;
+    bool have = false;
+    Part p;
+    uint32_t done = 0;
+    uint64_t events = 0;
+    const EvInst* Ip = &a.inst[0];
+    TView tv = t;
+    float inv_k = 0.0f;
+    unsigned long long kq_part = 0;
+    for (;;) {
+        /* hand input particles to idle lanes */
+        unsigned need = __ballot_sync(0xffffffffu, !have);
+        if (need && !exhausted) {
+            uint32_t n_need = __popc(need);
+            uint64_t avail = pool_end - pool_next;
+            uint64_t nb = 0, ne = 0;
+            if (avail < n_need) {
+                unsigned long long base = 0;
+                if (lane == 0) base = atomicAdd(claim, (unsigned long long)CHUNK);
+                base = __shfl_sync(0xffffffffu, base, 0);
+                if (base < n_in) { nb = base; ne = base + CHUNK < n_in ? base + CHUNK : n_in; }
+                else exhausted = true;
+            }
+            uint32_t rank = __popc(need & lt);
+            uint64_t idx = 0;
+            bool got = false;
+            if (!have) {
+                if (rank < avail) { idx = pool_next + rank; got = true; }
+                else if (rank - avail < ne - nb) { idx = nb + (rank - avail); got = true; }
+            }
+            uint64_t take = n_need;
+            if (take <= avail) pool_next += take;
+            else { uint64_t from_new = take - avail; pool_next = nb + from_new; pool_end = ne;
+                   if (pool_next > pool_end) pool_next = pool_end; }
+            if (got) {
+                if (SOURCE) {
+                    uint32_t inst = 0;
+                    if (!ONE) {
+                        uint32_t lo = 0, hi = a.n_inst;
+                        while (hi - lo > 1) {
+                            uint32_t mid = (lo + hi) >> 1;
+                            if (a.inst_begin[mid] <= idx) lo = mid; else hi = mid;
+                        }
+                        inst = lo;
                     }
-                    inst = lo;
-                }
-                const EvInst& I = a.inst[inst];
-                const GenState* st = I.st;
-                p.id = (uint32_t)idx;
-                p.inst = inst;
-                p.local = (uint32_t)(idx - I.hist_begin);
-                p.seq = 0;
-                p.rng = nr_pcg32_seeded(nr_generation_seed(I.seed, st->gen), p.local);
-                uint64_t nb = BANK ? st->n_bank : 0;
-                if (nb > 0) {
-                    const nraps_site* bank = I.bank[st->gen & 1];
-                    uint64_t j = ((uint64_t)p.local * nb) / I.N;
-                    nraps_site s = bank[j];
-                    p.x = s.x; p.g = s.group;
-                    p.mu = __fsub_rn(__fmul_rn(2.0f, u24(nr_pcg32_next(&p.rng))), 1.0f);
+                    const EvInst& I = a.inst[inst];
+                    const GenState* st = I.st;
+                    p.id = (uint32_t)idx;
+                    p.inst = inst;
+                    p.local = (uint32_t)(idx - I.hist_begin);
+                    p.seq = 0;
+                    p.rng = nr_pcg32_seeded(nr_generation_seed(I.seed, st->gen), p.local);
+                    uint64_t nbk = BANK ? st->n_bank : 0;
+                    if (nbk > 0) {
+                        const nraps_site* bank = I.bank[st->gen & 1];
+                        uint64_t j = ((uint64_t)p.local * nbk) / I.N;
+                        nraps_site s = bank[j];
+                        p.x = s.x; p.g = s.group;
+                        p.mu = __fsub_rn(__fmul_rn(2.0f, u24(nr_pcg32_next(&p.rng))), 1.0f);
+                    } else {
+                        uint32_t cell = I.fuel[((uint64_t)nr_pcg32_next(&p.rng) * I.nfuel) >> 32];
+                        float sub = u24(nr_pcg32_next(&p.rng));
+                        p.x = __fadd_rn(I.cleft[cell], __fmul_rn(sub, I.cdx[cell]));
+                        p.mu = __fsub_rn(__fmul_rn(2.0f, u24(nr_pcg32_next(&p.rng))), 1.0f);
+                        p.g = chi_group(I.chicdf + (uint32_t)I.cmat[cell] * I.G, I.G, u24(nr_pcg32_next(&p.rng)));
+                    }
+                    if (REC && inst == 0) a.rec[p.local].draws += (nbk > 0) ? 1 : 4;
                 } else {
-                    uint32_t cell = I.fuel[((uint64_t)nr_pcg32_next(&p.rng) * I.nfuel) >> 32];
-                    float sub = u24(nr_pcg32_next(&p.rng));
-                    p.x = __fadd_rn(I.cleft[cell], __fmul_rn(sub, I.cdx[cell]));
-                    p.mu = __fsub_rn(__fmul_rn(2.0f, u24(nr_pcg32_next(&p.rng))), 1.0f);
-                    p.g = chi_group(I.chicdf + (uint32_t)I.cmat[cell] * I.G, I.G, u24(nr_pcg32_next(&p.rng)));
+                    p.x = a.qx[qin][idx];
+                    p.mu = a.qmu[qin][idx];
+                    p.rng.state = a.qrng[qin][idx];
+                    p.id = a.qid[qin][idx];
+                    uint32_t pk = a.qpk[qin][idx];
+                    p.g = pk & 15u;
+                    p.inst = (pk >> 4) & 0xFFFu;
+                    p.seq = pk >> 16;
+                    const EvInst& I = a.inst[ONE ? 0 : p.inst];
+                    p.local = (uint32_t)(p.id - I.hist_begin);
+                    p.rng.inc = ((uint64_t)p.local << 1) | 1ULL;
                 }
-                if (REC && inst == 0) a.rec[p.local].draws += (nb > 0) ? 1 : 4;
-            } else {
-                p.x = a.qx[qin][idx];
-                p.mu = a.qmu[qin][idx];
-                p.rng.state = a.qrng[qin][idx];
-                p.id = a.qid[qin][idx];
-                uint32_t pk = a.qpk[qin][idx];
-                p.g = pk & 15u;
-                p.inst = (pk >> 4) & 0xFFFu;
-                p.seq = pk >> 16;
-                const EvInst& I = a.inst[ONE ? 0 : p.inst];
-                p.local = (uint32_t)(p.id - I.hist_begin);
-                p.rng.inc = ((uint64_t)p.local << 1) | 1ULL;
+                Ip = &a.inst[ONE ? 0 : p.inst];
+                if (!ONE) tv = global_view(*Ip);
+                inv_k = BANK ? Ip->st->inv_kf : 0.0f;
+                have = true;
+                done = 0;
+                events = 0;
+                kq_part = 0;
             }
-            const EvInst& I = a.inst[ONE ? 0 : p.inst];
-            TView tv = ONE ? t : global_view(I);
-            float inv_k = BANK ? I.st->inv_kf : 0.0f;
-            unsigned long long kq_part = 0;
-            alive = run_particle<EXACT, BANK, REC>(a, I, tv, p, K, inv_k, acc, kq_part);
-            if (!ONE && kq_part) atomicAdd(&I.st->kq, kq_part);
         }
-        /* compact survivors into the out queue */
-        uint32_t excl;
-        uint32_t total = nrdev::block_excl_scan(alive ? 1u : 0u, &excl, s_scan);
-        if (total) {
-            if (threadIdx.x == 0) s_base = atomicAdd(&a.qcount[pass], (unsigned long long)total);
-            __syncthreads();
-            if (alive) {
-                uint64_t o = s_base + excl;
-                a.qx[qout][o] = p.x;
-                a.qmu[qout][o] = p.mu;
-                a.qrng[qout][o] = p.rng.state;
-                a.qid[qout][o] = p.id;
-                a.qpk[qout][o] = p.g | (p.inst << 4) | (p.seq << 16);
+        if (!__any_sync(0xffffffffu, have)) break;
+        bool push = false;
+        if (have) {
+            int f = step_particle<EXACT, BANK, REC>(a, *Ip, tv, p, inv_k, acc, events, kq_part);
+            ++done;
+            if (f != 0) have = false;
+            else if (done >= K) { push = true; have = false; }
+            if (!have && !ONE && kq_part) { atomicAdd(&Ip->st->kq, kq_part); kq_part = 0; }
+        }
+        /* stage survivors; flush 32 at a time */
+        unsigned pm = __ballot_sync(0xffffffffu, push);
+        if (pm) {
+            if (push) {
+                uint32_t slot = staged + __popc(pm & lt);
+                sg.x[slot] = p.x; sg.mu[slot] = p.mu; sg.rng[slot] = p.rng.state;
+                sg.id[slot] = p.id; sg.pk[slot] = p.g | (p.inst << 4) | (p.seq << 16);
             }
-            __syncthreads();
+            staged += __popc(pm);
+            __syncwarp();
+            if (staged >= 32) {
+                flush_stage(a, sg, 32, pass, qout, lane);
+                __syncwarp();
+                uint32_t rest = staged - 32;
+                float x2 = 0.f, mu2 = 0.f; unsigned long long r2 = 0; uint32_t id2 = 0, pk2 = 0;
+                if (lane < rest) {
+                    x2 = sg.x[32 + lane]; mu2 = sg.mu[32 + lane]; r2 = sg.rng[32 + lane];
+                    id2 = sg.id[32 + lane]; pk2 = sg.pk[32 + lane];
+                }
+                __syncwarp();
+                if (lane < rest) { sg.x[lane] = x2; sg.mu[lane] = mu2; sg.rng[lane] = r2; sg.id[lane] = id2; sg.pk[lane] = pk2; }
+                __syncwarp();
+                staged = rest;
+            }
         }
+    }
+    if (staged) {
+        __syncwarp();
+        flush_stage(a, sg, staged, pass, qout, lane);
     }
     /* flush counters: one atomic per warp */
     unsigned long long kq = nrdev::warp_sum_u64(ONE ? acc.kq : 0ull);
     unsigned long long coll = nrdev::warp_sum_u64(acc.coll), virt = nrdev::warp_sum_u64(acc.virt);
     unsigned long long ab = nrdev::warp_sum_u64(acc.absorbed), lk = nrdev::warp_sum_u64(acc.leaked);
     unsigned long long cp = nrdev::warp_sum_u64(acc.capped);
-    if ((threadIdx.x & 31) == 0) {
+    if (lane == 0) {
         GenState* s = a.stats;
         if (ONE && kq) atomicAdd(&a.inst[0].st->kq, kq);
         if (coll) atomicAdd(&s->collisions, coll);
@@ -416,68 +512,13 @@ __global__ void ev_scatter(EvArgs a) {
             s.group = gi & 15u;
             s.pad = 0;
             I.bank[(I.st->gen + 1) & 1][pos] = s;
-            atomicAdd(&I.hist[s.cell], 1u);
+            atomicAdd(&I.hist[(uint64_t)s.cell * HIST_STRIDE], 1u);
         }
     }
 }
 
-/* one thread per (instance, cell): reads and clears the G tally bins */
-__global__ void ev_fin_bins(EvArgs a) {
-    for (uint64_t gc = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; gc < a.n_cells_total;
-         gc += (uint64_t)gridDim.x * blockDim.x) {
-        uint32_t inst = a.n_inst == 1 ? 0u : find_inst(a.cell_begin, a.n_inst, gc);
-        const EvInst& I = a.inst[inst];
-        const GenState* st = I.st;
-        uint64_t c = gc - I.cell_begin;
-        const uint64_t gen = st->gen;
-        if (gen >= I.generations) continue;
-        const bool active = gen >= I.skip;
-        const double fund = 1.0 / (double)(I.generations - I.skip);
-        const double k = st->k;
-        const double conversion = I.conv_const * k;
-        const double N = (double)I.N;
-        double dx = I.dx64[c];
-        uint32_t m = I.cmat[c];
-        double fs = 0.0;
-        for (uint32_t g = 0; g < I.G; ++g) {
-            uint64_t bin = (uint64_t)g * I.nc + c;
-            double tl = I.tally[bin];
-            I.tally[bin] = 0.0;
-            double flux = tl / (k * N * dx);
-            fs += I.nsf64[m + (uint64_t)I.M * g] * flux;
-            double phi = tl / (N * dx);
-            if (active) {
-                I.flux_acc[bin] += flux * conversion * fund;
-                I.flux_sum[bin] += phi;
-                I.flux_sq[bin] += phi * phi;
-            }
-        }
-        if (active) I.fs_acc[c] += fs * fund;
-        if (a.bank) {
-            uint32_t cnt = I.hist[c];
-            I.hist[c] = 0;
-            uint64_t B = a.offsets[I.hist_begin + I.N] - a.offsets[I.hist_begin];
-            if (cnt && B) {
-                double pr = (double)cnt / (double)B;
-                atomicAdd(&I.st->h_acc, -pr * nr_log(pr) * 1.4426950408889634);
-            }
-        }
-    }
-}
-
-__global__ void ev_fin_state(EvArgs a) {
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i == 0) {
-        for (uint32_t p = 0; p < MAX_PASSES + 2; ++p) a.qcount[p] = 0;
-        for (uint32_t s = 0; s < NSLAB; ++s) a.slab_count[s] = 0;
-        if (a.n_inst > 1) {
-            GenState* s = a.stats;
-            s->tot_collisions += s->collisions; s->tot_virtual += s->virtual_collisions;
-            s->tot_absorbed += s->absorbed; s->tot_leaked += s->leaked; s->tot_capped += s->capped;
-            s->collisions = s->virtual_collisions = s->absorbed = s->leaked = s->capped = 0;
-        }
-    }
-    if (i >= a.n_inst) return;
+/* per-instance end of generation: k, entropy, bank size, counters */
+__device__ void finish_instance(const EvArgs& a, uint32_t i) {
     const EvInst& I = a.inst[i];
     GenState* st = I.st;
     uint64_t gen = st->gen;
@@ -504,6 +545,96 @@ __global__ void ev_fin_state(EvArgs a) {
     st->k = k_new;
     st->inv_kf = (float)(1.0 / k_new);
     st->gen = gen + 1;
+}
+
+/*
+ * One thread per (instance, cell): reads and clears the cell's G tally bins,
+ * accumulates flux and fission source of active generations, and the cell's
+ * entropy term.  The last block to finish (threadfence + counter, no waiting)
+ * then closes the generation of every instance and resets the pass counters.
+ */
+__global__ void __launch_bounds__(256) ev_finalize(EvArgs a) {
+    __shared__ bool s_last;
+    for (uint64_t gc0 = (uint64_t)blockIdx.x * blockDim.x; gc0 < a.n_cells_total;
+         gc0 += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t gc = gc0 + threadIdx.x;
+        double h = 0.0;
+        uint32_t inst = 0xFFFFFFFFu;
+        if (gc < a.n_cells_total) {
+            inst = a.n_inst == 1 ? 0u : find_inst(a.cell_begin, a.n_inst, gc);
+            const EvInst& I = a.inst[inst];
+            const GenState* st = I.st;
+            uint64_t c = gc - I.cell_begin;
+            const uint64_t gen = st->gen;
+            if (gen < I.generations) {
+                const bool active = gen >= I.skip;
+                const double fund = 1.0 / (double)(I.generations - I.skip);
+                const double k = st->k;
+                const double conversion = I.conv_const * k;
+                const double N = (double)I.N;
+                double dx = I.dx64[c];
+                uint32_t m = I.cmat[c];
+                double fs = 0.0;
+                for (uint32_t g = 0; g < I.G; ++g) {
+                    uint64_t bin = (uint64_t)g * I.nc + c;
+                    double tl = I.tally[bin];
+                    I.tally[bin] = 0.0;
+                    double flux = tl / (k * N * dx);
+                    fs += I.nsf64[m + (uint64_t)I.M * g] * flux;
+                    double phi = tl / (N * dx);
+                    if (active) {
+                        I.flux_acc[bin] += flux * conversion * fund;
+                        I.flux_sum[bin] += phi;
+                        I.flux_sq[bin] += phi * phi;
+                    }
+                }
+                if (active) I.fs_acc[c] += fs * fund;
+                if (a.bank) {
+                    uint32_t cnt = I.hist[c * HIST_STRIDE];
+                    I.hist[c * HIST_STRIDE] = 0;
+                    uint64_t B = a.offsets[I.hist_begin + I.N] - a.offsets[I.hist_begin];
+                    if (cnt && B) {
+                        double pr = (double)cnt / (double)B;
+                        h = -pr * nr_log(pr) * 1.4426950408889634;
+                    }
+                }
+            }
+        }
+        if (a.bank) {
+            /* warps within one instance reduce first; mixed warps add per lane */
+            uint32_t i0 = __shfl_sync(0xffffffffu, inst, 0);
+            bool uniform = __all_sync(0xffffffffu, inst == i0);
+            if (uniform) {
+                for (int o = 16; o > 0; o >>= 1) h += __shfl_down_sync(0xffffffffu, h, o);
+                if ((threadIdx.x & 31) == 0 && i0 != 0xFFFFFFFFu && h != 0.0) atomicAdd(&a.inst[i0].st->h_acc, h);
+            } else if (inst != 0xFFFFFFFFu && h != 0.0) {
+                atomicAdd(&a.inst[inst].st->h_acc, h);
+            }
+        }
+    }
+    /* last block closes the generation */
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long d = atomicAdd(a.blocks_done, 1ULL);
+        s_last = (d == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    for (uint32_t i = threadIdx.x; i < a.n_inst; i += blockDim.x) finish_instance(a, i);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (uint32_t p = 0; p < 2 * (MAX_PASSES + 2); ++p) a.qcount[p] = 0;
+        for (uint32_t q = 0; q < NSLAB; ++q) a.slab_count[q] = 0;
+        if (a.n_inst > 1) {
+            GenState* s = a.stats;
+            s->tot_collisions += s->collisions; s->tot_virtual += s->virtual_collisions;
+            s->tot_absorbed += s->absorbed; s->tot_leaked += s->leaked; s->tot_capped += s->capped;
+            s->collisions = s->virtual_collisions = s->absorbed = s->leaked = s->capped = 0;
+        }
+        *a.blocks_done = 0;
+    }
 }
 
 template <class T> struct DBuf {
@@ -560,7 +691,7 @@ int EventEngine::configure(const nraps_opts& o, std::string& err) {
     if (o.block_size) params.block = o.block_size;
     if (o.events_per_pass) params.K = o.events_per_pass;
     if (o.passes) params.passes = o.passes;
-    if (params.block != 128 && params.block != 256 && params.block != 512) { err = "block_size must be 128, 256 or 512"; return NRAPS_ERR_INVALID; }
+    if (params.block != 128 && params.block != 256) { err = "block_size must be 128 or 256 for WOODCOCK"; return NRAPS_ERR_INVALID; }
     if (params.passes < 1 || params.passes > MAX_PASSES) { err = "passes must be in [1, 16]"; return NRAPS_ERR_INVALID; }
     if (params.K < 1) { err = "events_per_pass must be >= 1"; return NRAPS_ERR_INVALID; }
     impl_->committed = false;
@@ -704,14 +835,14 @@ int EventEngine::commit(cudaStream_t s, std::string& err) {
         A(m.count.alloc(m.n_total)); A(m.offsets.alloc(m.n_total + 1));
         A(m.block_sums.alloc((m.n_total + 4095) / 4096 + 1));
     }
-    if (!m.qcount.p) { A(m.qcount.alloc(MAX_PASSES + 2)); A(m.slab_count.alloc(NSLAB)); A(m.bstats.alloc(1)); }
+    if (!m.qcount.p) { A(m.qcount.alloc(2 * (MAX_PASSES + 2) + 2)); A(m.slab_count.alloc(NSLAB)); A(m.bstats.alloc(1)); }
     uint64_t want_slab = bank ? (bank_sum + 2 * m.n_total) / NSLAB + 4096 : 1;
     if (want_slab > m.slab_cap || !m.sx.p) {
         m.slab_cap = want_slab;
         uint64_t tot = NSLAB * m.slab_cap;
         A(m.sx.alloc(tot)); A(m.scell.alloc(tot)); A(m.sgi.alloc(tot)); A(m.sparent.alloc(tot)); A(m.sseq.alloc(tot));
     }
-    A(cudaMemsetAsync(m.qcount.p, 0, (MAX_PASSES + 2) * 8, s));
+    A(cudaMemsetAsync(m.qcount.p, 0, (2 * (MAX_PASSES + 2) + 2) * 8, s));
     A(cudaMemsetAsync(m.slab_count.p, 0, NSLAB * 8, s));
     A(cudaMemsetAsync(m.bstats.p, 0, sizeof(GenState), s));
     if (bank) A(cudaMemsetAsync(m.count.p, 0, m.n_total * 4, s));
@@ -723,6 +854,8 @@ int EventEngine::commit(cudaStream_t s, std::string& err) {
         a.qx[q] = m.qx[q].p; a.qmu[q] = m.qmu[q].p; a.qrng[q] = m.qrng[q].p; a.qid[q] = m.qid[q].p; a.qpk[q] = m.qpk[q].p;
     }
     a.qcount = m.qcount.p;
+    a.claim = m.qcount.p + (MAX_PASSES + 2);
+    a.blocks_done = m.qcount.p + 2 * (MAX_PASSES + 2);
     a.sx = m.sx.p; a.scell = m.scell.p; a.sgi = m.sgi.p; a.sparent = m.sparent.p; a.sseq = m.sseq.p;
     a.slab_count = m.slab_count.p; a.slab_cap = m.slab_cap;
     a.count = m.count.p; a.offsets = m.offsets.p;
@@ -798,9 +931,8 @@ int EventEngine::enqueue_generation(cudaStream_t s, bool with_finalize, cudaEven
     }
     if (with_finalize) {
         unsigned gb = (unsigned)std::min<uint64_t>((m.n_cells_total + 255) / 256, (uint64_t)m.grid_blocks * 2);
-        ev_fin_bins<<<gb ? gb : 1, 256, 0, s>>>(a);
-        ev_fin_state<<<(a.n_inst + 127) / 128, 128, 0, s>>>(a);
-        n += 2;
+        ev_finalize<<<gb ? gb : 1, 256, 0, s>>>(a);
+        n += 1;
     }
     return cudaPeekAtLastError() == cudaSuccess ? n : -1;
 }

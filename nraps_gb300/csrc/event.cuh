@@ -32,10 +32,12 @@ struct EvBuffers {
     double *k64, *entropy;                 /* generations                    */
     nraps_site* bank[2];                   /* BANK mode ordered banks        */
     uint64_t bank_cap;
-    uint32_t* hist;                        /* nc (BANK mode)                 */
+    uint32_t* hist;                        /* nc * EV_HIST_STRIDE (BANK mode)  */
     uint64_t generations, skip;
     uint64_t seed;
 };
+
+#define EV_HIST_STRIDE 32  /* entropy counters are 128 B apart */
 
 struct EvParams {
     uint32_t block = 256;   /* threads per block of the transport passes       */
