@@ -301,6 +301,39 @@ void nraps_meshbuf_free(nraps_meshbuf* m);
 /* Fill a problem view from parsed input + mesh (pointers alias them). */
 int  nraps_problem_view(const nraps_input* in, const nraps_meshbuf* mesh, nraps_problem* out);
 
+/* ---- one generation without allocating ----------------------------------
+   No counterpart in the reference: for callers that cannot allocate device
+   memory themselves at call time (an application whose device memory is all
+   handed out by its own pool, a pre-planned memory layout, a job that must
+   not fail on an allocation midway).  Runs one PHYSICS-mode generation of the
+   plain FP32 kernel on problem arrays that are already on the device and
+   writes the FP64 track-length tally (G*n_cells, row-major [g*n_cells + c])
+   and k (one double) into caller buffers on the caller's stream.  Its working
+   state lives in a fixed array inside the library (about 80 KB per device,
+   kept until the process exits); nothing is allocated.  Limits:
+   MatTypes*EnergyGroups <= 1024, MatTypes*EnergyGroups^2 <= 16384,
+   EnergyGroups <= 16; larger problems are rejected with NRAPS_ERR_INVALID.
+   The first call on a device looks up the array's device address; make it
+   before any stream capture.  Calls share the array: calls whose work
+   overlaps on the GPU race, so order them.  The call checks the device inputs
+   (one synchronisation of `stream`), then enqueues the generation and returns;
+   d_error (may be NULL) receives the generation's error bits (4 = a history
+   hit max_events).  Errors are reported through nraps_last_error(NULL). */
+typedef struct nraps_device_problem {
+    const float *sigt, *sigs, *mu, *siga, *sigf, *nut, *chit, *scat_matrix, *inv_sigtr;
+    const uint8_t* matid;
+    const float *delta_x, *mesh_left, *mesh_right;
+    const uint64_t* fuel_indices;
+    uint32_t mattypes, energygroups;
+    uint64_t n_cells, n_fuel, histories;
+    float boundl, boundr;
+} nraps_device_problem;
+
+int nraps_physics_generation_noalloc(const nraps_device_problem* p, uint64_t seed,
+                                     uint64_t generation, uint64_t max_events,
+                                     double* d_tally, double* d_k, uint32_t* d_error,
+                                     void* stream);
+
 /* Text of a status code. */
 const char* nraps_status_string(int status);
 

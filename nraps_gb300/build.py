@@ -9,8 +9,9 @@ Flags that carry meaning:
   -ffp-contract=off   host code: table arithmetic must round as written on
                       both x86_64 and aarch64 (GCC fuses multiply-adds on
                       aarch64 by default).
-  --fmad=false        plain.cu and bank.cu only: the plain kernel reproduces
-                      a CPU restatement bit for bit.
+  --fmad=false        plain.cu, bank.cu and noalloc.cu: the plain kernel and
+                      its derived tables reproduce a CPU restatement bit for
+                      bit.
 """
 from __future__ import annotations
 
@@ -32,6 +33,7 @@ CU_SOURCES = {
     "bank.cu": ["--fmad=false"],
     "engine.cu": [],
     "event.cu": [],
+    "noalloc.cu": ["--fmad=false"],
 }
 CPP_SOURCES = ["host_frontend.cpp", "tables.cpp"]
 
