@@ -301,6 +301,65 @@ void nraps_meshbuf_free(nraps_meshbuf* m);
 /* Fill a problem view from parsed input + mesh (pointers alias them). */
 int  nraps_problem_view(const nraps_input* in, const nraps_meshbuf* mesh, nraps_problem* out);
 
+/* ---- batched instances ----------------------------------------------------
+   Build-defined (the reference solves one problem per call).  Independent
+   slab problems of any size advance together: one launch sequence of the
+   WOODCOCK engine per generation for all of them (CUDA-graph replayed with
+   opts.use_graphs).  The context's options apply to every instance; seeds[i]
+   seeds instance i (NULL: opts.seed + i).  Every instance's results are the
+   ones it would get alone with the same seed. */
+typedef struct nraps_batch nraps_batch;
+int  nraps_batch_create(nraps_ctx* ctx, const nraps_problem* problems, uint32_t n,
+                        const uint64_t* seeds, nraps_batch** out);
+int  nraps_batch_run(nraps_batch* b, uint64_t n_generations);      /* async */
+int  nraps_batch_sync(nraps_batch* b);
+int  nraps_batch_results(nraps_batch* b, uint32_t i, nraps_result* out);
+/* device ms of all generations run, histories simulated, real collisions */
+int  nraps_batch_timing(nraps_batch* b, double* ms, uint64_t* histories, uint64_t* collisions);
+uint32_t nraps_batch_size(const nraps_batch* b);
+void nraps_batch_destroy(nraps_batch* b);
+
+/* ---- request server (continuous batching) ---------------------------------
+   Build-defined.  submit() queues a k-eigenvalue solve; each step() admits
+   queued requests while device slots and the HBM budget allow, runs one
+   generation of every admitted request together, and retires requests whose
+   standard error of k (over their active generations, at least min_active)
+   is at most sigma_k_target, or that reached their Generations cap.  Fission
+   banks and tallies stay on the device from admission until release(). */
+#define NRAPS_REQ_QUEUED   0
+#define NRAPS_REQ_RUNNING  1
+#define NRAPS_REQ_DONE     2
+#define NRAPS_REQ_REJECTED 3
+typedef struct nraps_server_opts {
+    uint64_t hbm_budget_bytes;   /* admission limit; 0 = 120 GiB               */
+    double   sigma_k_target;     /* absolute standard error of k (50 pcm = 5e-4) */
+    uint32_t min_active;         /* active generations before the test         */
+    uint32_t max_slots;          /* requests on the device at once, <= 4095    */
+    uint32_t reserved[4];
+} nraps_server_opts;
+typedef struct nraps_request_info {
+    uint64_t id;
+    int32_t  state;              /* NRAPS_REQ_*                                */
+    int32_t  status;             /* NRAPS_OK, or why it stopped                */
+    uint64_t generations_run;
+    uint64_t histories_per_generation;
+    double   k_mean, k_sigma;    /* over the active generations                */
+    double   t_submit, t_admit, t_done;  /* seconds on nraps_server_clock      */
+} nraps_request_info;
+typedef struct nraps_server nraps_server;
+void nraps_server_opts_default(nraps_server_opts* o);
+int  nraps_server_create(nraps_ctx* ctx, const nraps_server_opts* o, nraps_server** out);
+/* copies the problem; NRAPS_ERR_REJECTED if it can never fit the budget */
+int  nraps_server_submit(nraps_server* s, const nraps_problem* p, uint64_t seed, uint64_t* req_id);
+int  nraps_server_step(nraps_server* s, uint32_t* n_running, uint32_t* n_finished);
+/* NRAPS_ERR_PENDING while queued/running; fills out (may be NULL) when done */
+int  nraps_server_poll(nraps_server* s, uint64_t req_id, nraps_result* out, nraps_request_info* info);
+int  nraps_server_release(nraps_server* s, uint64_t req_id);
+int  nraps_server_stats(nraps_server* s, uint64_t* histories, uint64_t* completed, uint32_t* running,
+                        uint32_t* waiting, double* busy_ms, uint64_t* bytes_in_use);
+double nraps_server_clock(const nraps_server* s);
+void nraps_server_destroy(nraps_server* s);
+
 /* ---- one generation without allocating ----------------------------------
    No counterpart in the reference: for callers that cannot allocate device
    memory themselves at call time (an application whose device memory is all

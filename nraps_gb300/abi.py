@@ -313,3 +313,18 @@ class ResultArrays:
 
     def flux2d(self):
         return self.flux.reshape(self.G, self.cells)
+
+
+REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_REJECTED = 0, 1, 2, 3
+
+
+class ServerOpts(C.Structure):
+    _fields_ = [("hbm_budget_bytes", C.c_uint64), ("sigma_k_target", C.c_double),
+                ("min_active", C.c_uint32), ("max_slots", C.c_uint32), ("reserved", C.c_uint32 * 4)]
+
+
+class RequestInfo(C.Structure):
+    _fields_ = [("id", C.c_uint64), ("state", C.c_int32), ("status", C.c_int32),
+                ("generations_run", C.c_uint64), ("histories_per_generation", C.c_uint64),
+                ("k_mean", C.c_double), ("k_sigma", C.c_double),
+                ("t_submit", C.c_double), ("t_admit", C.c_double), ("t_done", C.c_double)]

@@ -84,6 +84,25 @@ def load(build_if_missing: bool = True):
                                  P(P(abi.MeshBuf))]
     L.nraps_meshbuf_free.argtypes = [P(abi.MeshBuf)]
     L.nraps_problem_view.argtypes = [P(abi.Input), P(abi.MeshBuf), P(abi.Problem)]
+    L.nraps_batch_create.argtypes = [vp, P(abi.Problem), C.c_uint32, P(C.c_uint64), P(vp)]
+    L.nraps_batch_run.argtypes = [vp, C.c_uint64]
+    L.nraps_batch_sync.argtypes = [vp]
+    L.nraps_batch_results.argtypes = [vp, C.c_uint32, P(abi.Result)]
+    L.nraps_batch_timing.argtypes = [vp, P(C.c_double), P(C.c_uint64), P(C.c_uint64)]
+    L.nraps_batch_size.argtypes = [vp]
+    L.nraps_batch_size.restype = C.c_uint32
+    L.nraps_batch_destroy.argtypes = [vp]
+    L.nraps_server_opts_default.argtypes = [P(abi.ServerOpts)]
+    L.nraps_server_create.argtypes = [vp, P(abi.ServerOpts), P(vp)]
+    L.nraps_server_submit.argtypes = [vp, P(abi.Problem), C.c_uint64, P(C.c_uint64)]
+    L.nraps_server_step.argtypes = [vp, P(C.c_uint32), P(C.c_uint32)]
+    L.nraps_server_poll.argtypes = [vp, C.c_uint64, P(abi.Result), P(abi.RequestInfo)]
+    L.nraps_server_release.argtypes = [vp, C.c_uint64]
+    L.nraps_server_stats.argtypes = [vp, P(C.c_uint64), P(C.c_uint64), P(C.c_uint32), P(C.c_uint32),
+                                     P(C.c_double), P(C.c_uint64)]
+    L.nraps_server_clock.argtypes = [vp]
+    L.nraps_server_clock.restype = C.c_double
+    L.nraps_server_destroy.argtypes = [vp]
     L.nraps_status_string.argtypes = [C.c_int]
     L.nraps_status_string.restype = C.c_char_p
     _LIB = L
@@ -377,3 +396,123 @@ def monte_carlo(variables, xsdata, delta_x, meshid, fuel_indices, k_new=1.0, *, 
     finally:
         if own:
             c.close()
+
+
+class Batch:
+    """Independent problems advancing together, one launch sequence per generation."""
+
+    def __init__(self, ctx: Context, problems, seeds=None):
+        self.ctx, self._L = ctx, ctx._L
+        self.problems = list(problems)
+        arr = (abi.Problem * len(self.problems))()
+        for i, p in enumerate(self.problems):
+            arr[i] = p.view()
+        self._arr = arr
+        sd = None
+        if seeds is not None:
+            self._seeds = np.ascontiguousarray(seeds, np.uint64)
+            sd = self._seeds.ctypes.data_as(C.POINTER(C.c_uint64))
+        h = C.c_void_p()
+        _check(self._L.nraps_batch_create(ctx.h, arr, len(self.problems), sd, C.byref(h)), ctx.h)
+        self.h = h
+
+    def run(self, n: int):
+        _check(self._L.nraps_batch_run(self.h, n), self.ctx.h)
+
+    def sync(self):
+        _check(self._L.nraps_batch_sync(self.h), self.ctx.h)
+
+    def results(self, i: int) -> ResultArrays:
+        p = self.problems[i]
+        res = ResultArrays(p.energygroups, p.n_cells, p.generations)
+        rv = res.view()
+        _check(self._L.nraps_batch_results(self.h, i, C.byref(rv)), self.ctx.h)
+        return res
+
+    def timing(self) -> dict:
+        ms, hist, coll = C.c_double(), C.c_uint64(), C.c_uint64()
+        _check(self._L.nraps_batch_timing(self.h, C.byref(ms), C.byref(hist), C.byref(coll)), self.ctx.h)
+        return dict(ms=ms.value, histories=hist.value, collisions=coll.value)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self._L.nraps_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """Continuous-batching request loop for k-eigenvalue solves."""
+
+    def __init__(self, ctx: Context, hbm_budget_bytes: int = 120 << 30, sigma_k_target: float = 50e-5,
+                 min_active: int = 10, max_slots: int = 1024):
+        self.ctx, self._L = ctx, ctx._L
+        o = abi.ServerOpts()
+        self._L.nraps_server_opts_default(C.byref(o))
+        o.hbm_budget_bytes, o.sigma_k_target = hbm_budget_bytes, sigma_k_target
+        o.min_active, o.max_slots = min_active, max_slots
+        h = C.c_void_p()
+        _check(self._L.nraps_server_create(ctx.h, C.byref(o), C.byref(h)), ctx.h)
+        self.h = h
+        self._problems = {}
+
+    def submit(self, prob: ProblemArrays, seed: int) -> int:
+        rid = C.c_uint64()
+        pv = prob.view()
+        _check(self._L.nraps_server_submit(self.h, C.byref(pv), seed, C.byref(rid)), self.ctx.h)
+        self._problems[rid.value] = prob
+        return rid.value
+
+    def step(self):
+        r, f = C.c_uint32(), C.c_uint32()
+        _check(self._L.nraps_server_step(self.h, C.byref(r), C.byref(f)), self.ctx.h)
+        return r.value, f.value
+
+    def poll(self, rid: int, results: bool = True):
+        """(status, info dict, ResultArrays or None); status ERR_PENDING while running."""
+        info = abi.RequestInfo()
+        res = None
+        rv_struct = None
+        if results:
+            p = self._problems[rid]
+            res = ResultArrays(p.energygroups, p.n_cells, p.generations)
+            rv_struct = res.view()
+        st = self._L.nraps_server_poll(self.h, rid, C.byref(rv_struct) if rv_struct is not None else None,
+                                       C.byref(info))
+        d = {f: getattr(info, f) for f, _ in abi.RequestInfo._fields_}
+        if st not in (abi.OK, abi.ERR_PENDING, abi.ERR_CAPPED):
+            _check(st, self.ctx.h)
+        return st, d, (res if st in (abi.OK, abi.ERR_CAPPED) else None)
+
+    def release(self, rid: int):
+        _check(self._L.nraps_server_release(self.h, rid), self.ctx.h)
+        self._problems.pop(rid, None)
+
+    def stats(self) -> dict:
+        h, c, b = C.c_uint64(), C.c_uint64(), C.c_uint64()
+        r, w = C.c_uint32(), C.c_uint32()
+        ms = C.c_double()
+        _check(self._L.nraps_server_stats(self.h, C.byref(h), C.byref(c), C.byref(r), C.byref(w), C.byref(ms),
+                                          C.byref(b)), self.ctx.h)
+        return dict(histories=h.value, completed=c.value, running=r.value, waiting=w.value, busy_ms=ms.value,
+                    bytes_in_use=b.value)
+
+    @property
+    def clock(self) -> float:
+        return float(self._L.nraps_server_clock(self.h))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self._L.nraps_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -34,6 +34,7 @@ CU_SOURCES = {
     "engine.cu": [],
     "event.cu": [],
     "noalloc.cu": ["--fmad=false"],
+    "serve.cu": [],
 }
 CPP_SOURCES = ["host_frontend.cpp", "tables.cpp"]
 

@@ -168,6 +168,7 @@ __global__ void finalize_state(FinalizeArgs a) {
     uint64_t gen = st->gen;
     if (gen < a.generations) {
         a.k64[gen] = k_new;
+        if (gen >= a.skip) { st->ksum += k_new; st->ksum2 += k_new * k_new; st->nactive++; }
         a.entropy[gen] = a.bank_mode ? hs : 0.0;
     }
     if (a.bank_mode) {

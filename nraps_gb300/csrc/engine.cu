@@ -25,6 +25,7 @@
 #include "event.cuh"
 #include "host_common.hpp"
 #include "tables.hpp"
+#include "engine_internal.hpp"
 
 /* ---- thread-local error text for calls without a context ---------------- */
 namespace nraps_host {
@@ -33,46 +34,19 @@ void set_error(const std::string& msg) { g_err = msg; }
 const char* last_error() { return g_err.c_str(); }
 }  // namespace nraps_host
 
-struct nraps_ctx {
-    nraps_opts opts;
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    std::string err;
-    uint64_t launches = 0;
-};
-
-namespace {
-
-int set_err(nraps_ctx* c, int code, const std::string& msg) {
-    if (c) c->err = msg; else nraps_host::set_error(msg);
-    return code;
-}
+using nrint::DevMem;
+using nrint::set_err;
 
 #define CK(call)                                                                        \
     do {                                                                                \
         cudaError_t e_ = (call);                                                        \
         if (e_ != cudaSuccess)                                                          \
-            return set_err(ctx, e_ == cudaErrorMemoryAllocation ? NRAPS_ERR_NOMEM : NRAPS_ERR_CUDA, \
-                           std::string(#call) + ": " + cudaGetErrorString(e_));         \
+            return set_err(ctx, nrint::cuda_status(e_), std::string(#call) + ": " + cudaGetErrorString(e_)); \
     } while (0)
 
-struct DevMem {
-    void* p = nullptr;
-    size_t n = 0;
-    DevMem() = default;
-    DevMem(const DevMem&) = delete;
-    DevMem& operator=(const DevMem&) = delete;
-    ~DevMem() { if (p) cudaFree(p); }
-    cudaError_t alloc(size_t bytes) {
-        if (p) { cudaFree(p); p = nullptr; }
-        n = bytes;
-        if (bytes == 0) return cudaSuccess;
-        return cudaMalloc(&p, bytes);
-    }
-    template <class T> T* as() const { return reinterpret_cast<T*>(p); }
-};
+namespace nrint {
 
-int validate(nraps_ctx* ctx, const nraps_problem* p, const nraps_opts& o) {
+int validate_problem(nraps_ctx* ctx, const nraps_problem* p, const nraps_opts& o) {
     if (!p) return set_err(ctx, NRAPS_ERR_INVALID, "problem is NULL");
     const nraps_variables& v = p->variables;
     if (o.abi_version != NRAPS_ABI_VERSION) return set_err(ctx, NRAPS_ERR_INVALID, "opts.abi_version mismatch");
@@ -96,6 +70,126 @@ int validate(nraps_ctx* ctx, const nraps_problem* p, const nraps_opts& o) {
     return NRAPS_OK;
 }
 
+cudaError_t InstBuffers::alloc(uint64_t G_, uint64_t nc_, uint64_t gens_, uint64_t N, double bank_factor, bool bank,
+                               double k0, GenState* st_ext, cudaStream_t s) {
+    G = G_; nc = nc_; gens = gens_;
+    double bf = bank_factor > 0 ? bank_factor : 3.0;
+    cap = bank ? (uint64_t)(bf * (double)N) + 1024 : 0;
+    uint64_t nb = G * nc;
+    cudaError_t e = cudaSuccess;
+    auto A = [&](cudaError_t x) { if (e == cudaSuccess) e = x; };
+    A(tally.alloc(nb * 8)); A(flux_acc.alloc(nb * 8)); A(flux_sum.alloc(nb * 8)); A(flux_sq.alloc(nb * 8));
+    A(fs_acc.alloc(nc * 8)); A(k64.alloc(gens * 8)); A(entropy.alloc(gens * 8));
+    if (bank) {
+        A(bank0.alloc(cap * sizeof(nraps_site))); A(bank1.alloc(cap * sizeof(nraps_site)));
+        A(hist.alloc(nc * EV_HIST_STRIDE * 4));
+        if (e == cudaSuccess) A(cudaMemsetAsync(hist.p, 0, nc * EV_HIST_STRIDE * 4, s));
+    }
+    if (st_ext) st = st_ext;
+    else { A(own_state.alloc(sizeof(GenState))); st = own_state.as<GenState>(); }
+    if (e != cudaSuccess) return e;
+    A(cudaMemsetAsync(tally.p, 0, nb * 8, s)); A(cudaMemsetAsync(flux_acc.p, 0, nb * 8, s));
+    A(cudaMemsetAsync(flux_sum.p, 0, nb * 8, s)); A(cudaMemsetAsync(flux_sq.p, 0, nb * 8, s));
+    A(cudaMemsetAsync(fs_acc.p, 0, nc * 8, s)); A(cudaMemsetAsync(k64.p, 0, gens * 8, s));
+    A(cudaMemsetAsync(entropy.p, 0, gens * 8, s));
+    GenState g0;
+    std::memset(&g0, 0, sizeof g0);
+    g0.k = k0;
+    g0.inv_kf = (float)(1.0 / k0);
+    A(cudaMemcpyAsync(st, &g0, sizeof g0, cudaMemcpyHostToDevice, s));
+    /* the host copy must outlive the async copy */
+    A(cudaStreamSynchronize(s));
+    return e;
+}
+
+EvBuffers InstBuffers::view(uint64_t skip, uint64_t seed) const {
+    EvBuffers b;
+    b.st = st; b.tally = tally.as<double>();
+    b.flux_acc = flux_acc.as<double>(); b.fs_acc = fs_acc.as<double>();
+    b.flux_sum = flux_sum.as<double>(); b.flux_sq = flux_sq.as<double>();
+    b.k64 = k64.as<double>(); b.entropy = entropy.as<double>();
+    b.bank[0] = bank0.as<nraps_site>(); b.bank[1] = bank1.as<nraps_site>();
+    b.bank_cap = cap; b.hist = hist.as<uint32_t>();
+    b.generations = gens; b.skip = skip; b.seed = seed;
+    return b;
+}
+
+int fetch_results(nraps_ctx* ctx, const ResultsView& v, nraps_result* out) {
+    uint64_t nb = v.G * v.nc, gens = v.gens, done = v.done, skip = v.skip;
+    std::vector<double> flux(nb), fsum(nb), fsq(nb), fs(v.nc), k64(gens), ent(gens);
+    CK(cudaMemcpy(flux.data(), v.flux_acc, nb * 8, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(fsum.data(), v.flux_sum, nb * 8, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(fsq.data(), v.flux_sq, nb * 8, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(fs.data(), v.fs_acc, v.nc * 8, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(k64.data(), v.k64, gens * 8, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(ent.data(), v.entropy, gens * 8, cudaMemcpyDeviceToHost));
+    GenState g;
+    CK(cudaMemcpy(&g, v.st, sizeof g, cudaMemcpyDeviceToHost));
+    std::vector<float> fl(nb), kf(gens, 0.0f), kk(gens, 0.0f);
+    for (uint64_t i = 0; i < nb; ++i) fl[i] = (float)flux[i];
+    for (uint64_t i = 0; i < gens; ++i) kk[i] = (float)k64[i];
+    if (out->flux) std::memcpy(out->flux, fl.data(), nb * 4);
+    if (out->fission_source) for (uint64_t c = 0; c < v.nc; ++c) out->fission_source[c] = (float)fs[c];
+    if (out->k) std::memcpy(out->k, kk.data(), gens * 4);
+    /* average_assembly (src/mc_code.rs:259-274), on the f32 flux */
+    if (out->assembly_average) {
+        std::vector<float> avg(nb, 0.0f);
+        uint64_t na = v.numass ? v.numass : 1, ma = v.nc / na;
+        for (uint64_t e = 0; e < v.G; ++e)
+            for (uint64_t a = 1; a <= na && ma > 0; ++a) {
+                float sum = 0.0f;
+                for (uint64_t i = (a - 1) * ma; i < a * ma; ++i) sum += fl[e * v.nc + i];
+                float av = sum / (float)ma;
+                for (uint64_t i = (a - 1) * ma; i < a * ma; ++i) avg[e * v.nc + i] = av;
+            }
+        std::memcpy(out->assembly_average, avg.data(), nb * 4);
+    }
+    /* k_fund (src/mc_code.rs:368-376), running mean of k over active gens */
+    if (skip < done) {
+        double run = 0.0;
+        for (uint64_t i = skip; i < done; ++i) { run += k64[i]; kf[i] = (float)(run / (double)(i - skip + 1)); }
+    }
+    if (out->k_fund) std::memcpy(out->k_fund, kf.data(), gens * 4);
+    if (out->k64) std::memcpy(out->k64, k64.data(), gens * 8);
+    if (out->entropy) std::memcpy(out->entropy, ent.data(), gens * 8);
+    uint64_t na = done > skip ? done - skip : 0;
+    if (out->flux_mean || out->flux_sem) {
+        for (uint64_t i = 0; i < nb; ++i) {
+            double m = na ? fsum[i] / (double)na : 0.0;
+            double var = na > 1 ? std::max(0.0, fsq[i] / (double)na - m * m) / (double)(na - 1) : 0.0;
+            if (out->flux_mean) out->flux_mean[i] = m;
+            if (out->flux_sem) out->flux_sem[i] = std::sqrt(var);
+        }
+    }
+    if (out->stats) {
+        nraps_stats& t = *out->stats;
+        std::memset(&t, 0, sizeof t);
+        if (na) {
+            double sum = 0, sq = 0;
+            for (uint64_t i = skip; i < done; ++i) { sum += k64[i]; sq += k64[i] * k64[i]; }
+            t.k_mean = sum / (double)na;
+            t.k_sigma = na > 1 ? std::sqrt(std::max(0.0, sq / (double)na - t.k_mean * t.k_mean) / (double)(na - 1)) : 0.0;
+        }
+        t.histories = v.histories;
+        t.collisions = g.tot_collisions; t.virtual_collisions = g.tot_virtual;
+        t.crossings = g.tot_crossings; t.absorbed = g.tot_absorbed; t.leaked = g.tot_leaked;
+        t.capped = g.tot_capped; t.sites = g.tot_sites;
+        t.transport_ms = v.transport_ms; t.total_ms = v.total_ms;
+        t.transport_launches = v.transport_launches;
+        t.gpu_launches = v.gpu_launches;
+    }
+    return NRAPS_OK;
+}
+
+uint64_t InstBuffers::bytes() const {
+    return tally.n + flux_acc.n + flux_sum.n + flux_sq.n + fs_acc.n + k64.n + entropy.n + bank0.n + bank1.n +
+           hist.n + own_state.n;
+}
+
+}  // namespace nrint
+
+namespace {
+using nrint::validate_problem;
 }  // namespace
 
 struct nraps_session {
@@ -159,7 +253,7 @@ void fill_plain(nraps_session* s, PlainArgs<T>& a) {
 
 int create_session(nraps_ctx* ctx, const nraps_problem* p, bool with_records, nraps_session** out) {
     *out = nullptr;
-    int st = validate(ctx, p, ctx->opts);
+    int st = validate_problem(ctx, p, ctx->opts);
     if (st) return st;
     std::unique_ptr<nraps_session> s(new nraps_session());
     s->ctx = ctx;
@@ -553,75 +647,18 @@ int nraps_session_timing(nraps_session* s, double* transport_ms, double* total_m
 
 int nraps_session_results(nraps_session* s, nraps_result* out) {
     if (!s || !out) return set_err(s ? s->ctx : nullptr, NRAPS_ERR_INVALID, "NULL argument");
-    nraps_ctx* ctx = s->ctx;
     int st = nraps_session_sync(s);
     if (st) return st;
-    uint64_t nb = s->G * s->nc, gens = s->gens, done = std::min(s->enqueued, gens);
-    std::vector<double> flux(nb), fsum(nb), fsq(nb), fs(s->nc), k64(gens), ent(gens);
-    CK(cudaMemcpy(flux.data(), s->flux_acc.p, nb * 8, cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(fsum.data(), s->flux_sum.p, nb * 8, cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(fsq.data(), s->flux_sq.p, nb * 8, cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(fs.data(), s->fs_acc.p, s->nc * 8, cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(k64.data(), s->k64.p, gens * 8, cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(ent.data(), s->entropy.p, gens * 8, cudaMemcpyDeviceToHost));
-    GenState g;
-    st = read_state(s, g);
-    if (st) return st;
-    std::vector<float> fl(nb), kf(gens, 0.0f), kk(gens, 0.0f);
-    for (uint64_t i = 0; i < nb; ++i) fl[i] = (float)flux[i];
-    for (uint64_t i = 0; i < gens; ++i) kk[i] = (float)k64[i];
-    if (out->flux) std::memcpy(out->flux, fl.data(), nb * 4);
-    if (out->fission_source) for (uint64_t c = 0; c < s->nc; ++c) out->fission_source[c] = (float)fs[c];
-    if (out->k) std::memcpy(out->k, kk.data(), gens * 4);
-    /* average_assembly (src/mc_code.rs:259-274), on the f32 flux */
-    if (out->assembly_average) {
-        std::vector<float> avg(nb, 0.0f);
-        uint64_t na = s->v.numass ? s->v.numass : 1, ma = s->nc / na;
-        for (uint64_t e = 0; e < s->G; ++e)
-            for (uint64_t a = 1; a <= na && ma > 0; ++a) {
-                float sum = 0.0f;
-                for (uint64_t i = (a - 1) * ma; i < a * ma; ++i) sum += fl[e * s->nc + i];
-                float av = sum / (float)ma;
-                for (uint64_t i = (a - 1) * ma; i < a * ma; ++i) avg[e * s->nc + i] = av;
-            }
-        std::memcpy(out->assembly_average, avg.data(), nb * 4);
-    }
-    /* k_fund (src/mc_code.rs:368-376), running mean of k over active gens */
-    uint64_t skip = s->v.skip;
-    if (skip < done) {
-        double run = 0.0;
-        for (uint64_t i = skip; i < done; ++i) { run += k64[i]; kf[i] = (float)(run / (double)(i - skip + 1)); }
-    }
-    if (out->k_fund) std::memcpy(out->k_fund, kf.data(), gens * 4);
-    if (out->k64) std::memcpy(out->k64, k64.data(), gens * 8);
-    if (out->entropy) std::memcpy(out->entropy, ent.data(), gens * 8);
-    uint64_t na = done > skip ? done - skip : 0;
-    if (out->flux_mean || out->flux_sem) {
-        for (uint64_t i = 0; i < nb; ++i) {
-            double m = na ? fsum[i] / (double)na : 0.0;
-            double var = na > 1 ? std::max(0.0, fsq[i] / (double)na - m * m) / (double)(na - 1) : 0.0;
-            if (out->flux_mean) out->flux_mean[i] = m;
-            if (out->flux_sem) out->flux_sem[i] = std::sqrt(var);
-        }
-    }
-    if (out->stats) {
-        nraps_stats& t = *out->stats;
-        std::memset(&t, 0, sizeof t);
-        if (na) {
-            double sum = 0, sq = 0;
-            for (uint64_t i = skip; i < done; ++i) { sum += k64[i]; sq += k64[i] * k64[i]; }
-            t.k_mean = sum / (double)na;
-            t.k_sigma = na > 1 ? std::sqrt(std::max(0.0, sq / (double)na - t.k_mean * t.k_mean) / (double)(na - 1)) : 0.0;
-        }
-        t.histories = s->enqueued * s->n_hist;
-        t.collisions = g.tot_collisions; t.virtual_collisions = g.tot_virtual;
-        t.crossings = g.tot_crossings; t.absorbed = g.tot_absorbed; t.leaked = g.tot_leaked;
-        t.capped = g.tot_capped; t.sites = g.tot_sites;
-        t.transport_ms = s->transport_ms; t.total_ms = s->total_ms;
-        t.transport_launches = s->transport_launches;
-        t.gpu_launches = ctx->launches;
-    }
-    return NRAPS_OK;
+    nrint::ResultsView v;
+    v.G = s->G; v.nc = s->nc; v.gens = s->gens; v.skip = s->v.skip; v.numass = s->v.numass;
+    v.done = std::min(s->enqueued, s->gens); v.histories = s->enqueued * s->n_hist;
+    v.flux_acc = s->flux_acc.as<double>(); v.flux_sum = s->flux_sum.as<double>();
+    v.flux_sq = s->flux_sq.as<double>(); v.fs_acc = s->fs_acc.as<double>();
+    v.k64 = s->k64.as<double>(); v.entropy = s->entropy.as<double>();
+    v.st = s->state.as<GenState>();
+    v.transport_ms = s->transport_ms; v.total_ms = s->total_ms;
+    v.transport_launches = s->transport_launches; v.gpu_launches = s->ctx->launches;
+    return nrint::fetch_results(s->ctx, v, out);
 }
 
 int nraps_solve(nraps_ctx* ctx, const nraps_problem* problem, nraps_result* out) {

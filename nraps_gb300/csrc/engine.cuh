@@ -41,6 +41,10 @@ struct GenState {
     /* run totals */
     unsigned long long tot_collisions, tot_virtual, tot_crossings, tot_absorbed,
         tot_leaked, tot_capped, tot_sites, tot_histories;
+    /* k over the active generations so far: sum, sum of squares, count */
+    double ksum, ksum2;
+    unsigned long long nactive;
+    unsigned long long pad2;
 };
 
 /* Unordered site stream written by the transport kernels. */

@@ -1,0 +1,82 @@
+/*
+ * engine_internal.hpp — host-side pieces shared by sessions, batches and the
+ * request server: the context, device buffers of one problem instance, and
+ * the conversion of an instance's FP64 device results into SolutionResults.
+ */
+#ifndef NRAPS_ENGINE_INTERNAL_HPP
+#define NRAPS_ENGINE_INTERNAL_HPP
+
+#include <cuda_runtime.h>
+
+#include <string>
+
+#include "../../include/nraps_gpu.h"
+#include "engine.cuh"
+#include "event.cuh"
+#include "host_common.hpp"
+
+struct nraps_ctx {
+    nraps_opts opts;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    uint64_t launches = 0;
+};
+
+namespace nrint {
+
+inline int set_err(nraps_ctx* c, int code, const std::string& msg) {
+    if (c) c->err = msg; else nraps_host::set_error(msg);
+    return code;
+}
+
+inline int cuda_status(cudaError_t e) {
+    return e == cudaErrorMemoryAllocation ? NRAPS_ERR_NOMEM : NRAPS_ERR_CUDA;
+}
+
+struct DevMem {
+    void* p = nullptr;
+    size_t n = 0;
+    DevMem() = default;
+    DevMem(const DevMem&) = delete;
+    DevMem& operator=(const DevMem&) = delete;
+    ~DevMem() { if (p) cudaFree(p); }
+    cudaError_t alloc(size_t bytes) {
+        if (p) { cudaFree(p); p = nullptr; }
+        n = bytes;
+        if (bytes == 0) return cudaSuccess;
+        return cudaMalloc(&p, bytes);
+    }
+    template <class T> T* as() const { return reinterpret_cast<T*>(p); }
+};
+
+/* Device buffers of one problem instance of the event engine. */
+struct InstBuffers {
+    DevMem tally, flux_acc, flux_sum, flux_sq, fs_acc, k64, entropy, bank0, bank1, hist, own_state;
+    GenState* st = nullptr;
+    uint64_t G = 0, nc = 0, gens = 0, cap = 0;
+    /* st_ext: a GenState slot owned by the caller, or nullptr to own one */
+    cudaError_t alloc(uint64_t G_, uint64_t nc_, uint64_t gens_, uint64_t N, double bank_factor, bool bank,
+                      double k0, GenState* st_ext, cudaStream_t s);
+    EvBuffers view(uint64_t skip, uint64_t seed) const;
+    uint64_t bytes() const;
+};
+
+/* What is needed to turn an instance's device results into SolutionResults. */
+struct ResultsView {
+    uint64_t G, nc, gens, skip, numass, done, histories;
+    const double *flux_acc, *flux_sum, *flux_sq, *fs_acc, *k64, *entropy;
+    const GenState* st;
+    double transport_ms, total_ms;
+    uint64_t transport_launches, gpu_launches;
+};
+
+/* Copies device results into `out` (synchronous on the current device). */
+int fetch_results(nraps_ctx* ctx, const ResultsView& v, nraps_result* out);
+
+/* Problem validation shared by every entry point. */
+int validate_problem(nraps_ctx* ctx, const nraps_problem* p, const nraps_opts& o);
+
+}  // namespace nrint
+
+#endif

@@ -7,16 +7,18 @@
  * majorant over the instance's materials; the flight is real with probability
  * sigtr(x)/maj[g], else virtual.  Real collisions score the collision
  * estimators (flux 1/sigtr into the tally cell, k score nu*sigf/sigtr in
- * 2^-32 fixed point), bank floor(nu*sigf/sigtr/k + u) sites (BANK mode),
- * then absorb with probability siga/sigtr or scatter (transport-corrected
- * CDF, isotropic mu).  Outer boundaries: vacuum leaks, reflective mirrors.
+ * 2^-32 fixed point, both precomputed per material and group), bank
+ * floor(nu*sigf/sigtr/k + u) sites (BANK mode), then absorb with probability
+ * siga/sigtr or scatter (transport-corrected CDF, isotropic mu).  Outer
+ * boundaries: vacuum leaks, reflective mirrors the position.
  *
- * Single-instance launches stage the instance's tables (cross sections,
- * CDFs, majorants, region bounds, materials and lookup grid) in shared
- * memory; batched launches read each particle's instance tables through L1.
- * Survivors are compacted per block (one atomic per block per grid-stride
- * step); fission sites go to one of 128 slabs (one atomic per group of
- * converged lanes, spread over 128 counters).
+ * Warps work independently: each iteration every live lane flies once (the
+ * flight is virtual or ends in a real collision); lanes whose particle died
+ * take the next input particle (claimed 64 at a time per warp); particles
+ * that completed K real collisions and new fission sites are staged per warp
+ * in shared memory and flushed 32 at a time with one atomic each.
+ * Single-instance launches stage the instance's tables in shared memory;
+ * batched launches read each particle's instance tables through L1.
  */
 #include <algorithm>
 #include <cstring>
@@ -32,25 +34,27 @@ constexpr uint32_t NSLAB = 128;
 constexpr uint32_t MAX_PASSES = 16;
 /* one entropy counter per 128-byte line: the fuel cells' site counts then
    spread over every L2 slice instead of a few dozen lines */
-constexpr uint32_t HIST_STRIDE = 32;
+constexpr uint32_t HIST_STRIDE = EV_HIST_STRIDE;
 
 struct EvInst {
-    const float* xs;        /* [(m*G+g)*4]: sigtr, pabs, nsf_st, inv_st        */
-    const float* scdf;      /* [(m*G+g)*G + e]                                 */
-    const float* chicdf;    /* [m*G + g]                                       */
-    const float* maj;       /* [g] majorant, [G+g] inverse                     */
-    const float* rleft;     /* R+1                                             */
-    const float* rinvdx;    /* R                                               */
-    const uint8_t* rmat;    /* R                                               */
-    const uint32_t* rfirst; /* R                                               */
-    const uint32_t* rncell; /* R                                               */
-    const uint16_t* grid;   /* nbins                                           */
-    const uint32_t* fuel;   /* nfuel                                           */
-    const float* cleft;     /* nc                                              */
-    const float* cdx;       /* nc                                              */
-    const uint8_t* cmat;    /* nc                                              */
-    const double* nsf64;    /* [m + M*g]                                       */
-    const double* dx64;     /* nc                                              */
+    const float* xs;          /* [(m*G+g)*4]: sigtr, pabs, nsf_st, inv_st      */
+    const double* inv_st64;   /* [m*G+g] flux score                            */
+    const unsigned long long* kq; /* [m*G+g] k score in 2^-32 fixed point      */
+    const float* scdf;        /* [(m*G+g)*G + e]                               */
+    const float* chicdf;      /* [m*G + g]                                     */
+    const float* maj;         /* [g] majorant, [G+g] inverse                   */
+    const float* rleft;       /* R+1                                           */
+    const float* rinvdx;      /* R                                             */
+    const uint8_t* rmat;      /* R                                             */
+    const uint32_t* rfirst;   /* R                                             */
+    const uint32_t* rncell;   /* R                                             */
+    const uint16_t* grid;     /* nbins                                         */
+    const uint32_t* fuel;     /* nfuel                                         */
+    const float* cleft;       /* nc                                            */
+    const float* cdx;         /* nc                                            */
+    const uint8_t* cmat;      /* nc                                            */
+    const double* nsf64;      /* [m + M*g]                                     */
+    const double* inv_dx64;   /* nc                                            */
     uint32_t M, G, R, nc, nbins, nfuel;
     float L, inv_binw, boundl, boundr;
     uint64_t hist_begin, N, seed;
@@ -78,11 +82,7 @@ struct EvArgs {
     unsigned long long* qcount;   /* MAX_PASSES+2: particles queued by pass p */
     unsigned long long* claim;    /* MAX_PASSES+2: input claimed by pass p    */
     unsigned long long* blocks_done; /* finalize: blocks that finished          */
-    float* sx;
-    uint32_t* scell;
-    uint32_t* sgi;                /* group | inst << 4                        */
-    uint32_t* sparent;
-    uint32_t* sseq;
+    uint4* sites;                 /* NSLAB slabs of slab_cap site records      */
     unsigned long long* slab_count;
     uint64_t slab_cap;
     uint32_t* count;
@@ -96,6 +96,8 @@ struct EvArgs {
 /* table view: shared memory (single instance) or the instance's globals */
 struct TView {
     const float* xs;
+    const double* inv_st64;
+    const unsigned long long* kq;
     const float* scdf;
     const float* chi;
     const float* maj;
@@ -126,16 +128,18 @@ __device__ __forceinline__ uint32_t region_of(const TView& t, float x) {
     return r;
 }
 
-/* partition_point(cdf[e] < v), clamped to G-1 (chi sampling, as energy()) */
-__device__ __forceinline__ uint32_t chi_group(const float* cdf, uint32_t G, float v) {
-    uint32_t base = 0, size = G;
-    while (size > 1) {
-        uint32_t half = size / 2, mid = base + half;
-        if (cdf[mid] < v) base = mid;
-        size -= half;
-    }
-    uint32_t r = base + ((cdf[base] < v) ? 1u : 0u);
-    return r < G - 1 ? r : G - 1;
+/* number of CDF entries below v, clamped to G-1: the chi group of energy()
+   (partition_point on a non-decreasing CDF), without data-dependent branches */
+__device__ __forceinline__ uint32_t count_below(const float* cdf, uint32_t G, float v) {
+    uint32_t n = 0;
+    for (uint32_t e = 0; e < G; ++e) n += (cdf[e] < v) ? 1u : 0u;
+    return n < G - 1 ? n : G - 1;
+}
+/* first e with v < cdf[e] (G-1 if none) == number of the first G-1 entries <= v */
+__device__ __forceinline__ uint32_t count_le(const float* cdf, uint32_t G, float v) {
+    uint32_t n = 0;
+    for (uint32_t e = 0; e + 1 < G; ++e) n += (cdf[e] <= v) ? 1u : 0u;
+    return n;
 }
 
 struct Part {
@@ -149,131 +153,38 @@ struct Acc {
     uint32_t coll, virt, absorbed, leaked, capped;
 };
 
-/* One flight to the next real collision and that collision.
-   Returns 0 while the particle lives, else its NRAPS_FATE_* + 1. */
-template <bool EXACT, bool BANK, bool REC>
-__device__ __forceinline__ int step_particle(const EvArgs& a, const EvInst& I, const TView& t, Part& p,
-                                             float inv_k, Acc& acc, uint64_t& events,
-                                             unsigned long long& kq_part) {
-    const uint32_t G = t.G;
-    uint32_t draws = 0;
-    auto next = [&]() -> uint32_t { if (REC) ++draws; return nr_pcg32_next(&p.rng); };
-    nraps_history_record* rec = (REC && p.inst == 0) ? &a.rec[p.local] : nullptr;
-    int fate = -1;
-    uint32_t r = 0, m = 0;
-    for (;;) {
-        if (++events > a.max_events) { fate = NRAPS_FATE_CAPPED; break; }
-        float d = __fmul_rn(neg_log<EXACT>(u24pos(next())), t.maj[G + p.g]);
-        p.x = __fadd_rn(p.x, __fmul_rn(p.mu, d));
-        int bounce = 0;
-        while (!(p.x >= 0.0f && p.x <= t.L)) {
-            if (p.x > t.L) {
-                if (t.boundr > 0.0f) { p.x = __fsub_rn(t.L, __fsub_rn(p.x, t.L)); p.mu = -p.mu; }
-                else { fate = NRAPS_FATE_LEAKED; break; }
-            } else {
-                if (t.boundl > 0.0f) { p.x = -p.x; p.mu = -p.mu; }
-                else { fate = NRAPS_FATE_LEAKED; break; }
-            }
-            if (++bounce > 1000) { fate = NRAPS_FATE_CAPPED; break; }
-        }
-        if (fate >= 0) break;
-        r = region_of(t, p.x);
-        m = t.rmat[r];
-        if (__fmul_rn(u24(next()), t.maj[p.g]) < t.xs[(m * G + p.g) * 4]) break;
-        acc.virt++;
-        if (REC && rec) rec->crossings++;
-    }
-    if (fate < 0) {
-        /* real collision */
-        acc.coll++;
-        const float4 X = *reinterpret_cast<const float4*>(&t.xs[(m * G + p.g) * 4]);
-        float rel = __fmul_rn(__fsub_rn(p.x, t.left[r]), t.invdx[r]);
-        uint32_t nr = t.ncell[r];
-        uint32_t k = rel > 0.0f ? (uint32_t)rel : 0u;
-        if (k >= nr) k = nr - 1;
-        uint32_t cell = t.first[r] + k;
-        atomicAdd(&I.tally[(uint64_t)p.g * I.nc + cell], (double)X.w);
-        unsigned long long q = nr_fix((double)X.z);
-        acc.kq += q;
-        kq_part += q;
-        if (REC && rec) {
-            rec->collisions++; rec->track += (double)X.w; rec->nsf_track += (double)X.z;
-            rec->final_cell = cell;
-        }
-        if (BANK) {
-            float nu = __fadd_rn(__fmul_rn(X.z, inv_k), u24(next()));
-            int n = (int)floorf(nu);
-            if (n > 64) n = 64;
-            for (int i = 0; i < n; ++i) {
-                uint32_t sg = chi_group(t.chi + m * G, G, u24(next()));
-                uint32_t slab = (blockIdx.x * 8 + (threadIdx.x >> 5)) % NSLAB;
-                unsigned long long j = nrdev::agg_inc(&a.slab_count[slab]);
-                if (j < a.slab_cap && p.seq < 0xFFFFu) {
-                    uint64_t at = (uint64_t)slab * a.slab_cap + j;
-                    a.sx[at] = p.x;
-                    a.scell[at] = cell;
-                    a.sgi[at] = sg | (p.inst << 4);
-                    a.sparent[at] = p.id;
-                    a.sseq[at] = p.seq;
-                } else {
-                    atomicOr(&I.st->error, NR_ERR_CAPACITY);
-                }
-                p.seq++;
-            }
-        }
-        if (u24(next()) < X.y) {
-            fate = NRAPS_FATE_ABSORBED;
-        } else {
-            float xi = u24(next());
-            const float* cdf = t.scdf + (m * G + p.g) * G;
-            uint32_t ng = G - 1;
-            for (uint32_t e = 0; e + 1 < G; ++e) if (xi < cdf[e]) { ng = e; break; }
-            p.g = ng;
-            p.mu = __fsub_rn(__fmul_rn(2.0f, u24(next())), 1.0f);
-        }
-    }
-    if (REC && rec) rec->draws += draws;
-    if (fate < 0) return 0;
-    if (fate == NRAPS_FATE_ABSORBED) acc.absorbed++;
-    else if (fate == NRAPS_FATE_LEAKED) acc.leaked++;
-    else { acc.capped++; atomicOr(&I.st->error, NR_ERR_CAPPED); }
-    if (BANK) a.count[p.id] = p.seq;
-    if (REC && rec) {
-        rec->fate = fate; rec->final_group = p.g; rec->final_x = (double)p.x;
-        rec->n_sites = p.seq;
-    }
-    return fate + 1;
-}
-
 __device__ __forceinline__ TView global_view(const EvInst& I) {
     TView t;
-    t.xs = I.xs; t.scdf = I.scdf; t.chi = I.chicdf; t.maj = I.maj; t.left = I.rleft;
-    t.grid = I.grid; t.rmat = I.rmat; t.invdx = I.rinvdx; t.first = I.rfirst; t.ncell = I.rncell;
+    t.xs = I.xs; t.inv_st64 = I.inv_st64; t.kq = I.kq; t.scdf = I.scdf; t.chi = I.chicdf; t.maj = I.maj;
+    t.left = I.rleft; t.grid = I.grid; t.rmat = I.rmat; t.invdx = I.rinvdx; t.first = I.rfirst;
+    t.ncell = I.rncell;
     t.G = I.G; t.R = I.R; t.nbins = I.nbins; t.L = I.L; t.inv_binw = I.inv_binw;
     t.boundl = I.boundl; t.boundr = I.boundr;
     return t;
 }
 
 /* shared-memory footprint of one instance's tables */
-__host__ __device__ __forceinline__ size_t smem_words(uint32_t M, uint32_t G, uint32_t R, uint32_t nbins) {
-    size_t f = (size_t)M * G * 4 + (size_t)M * G * G + (size_t)M * G + 2 * G + (R + 1) + 3 * (size_t)R;
-    size_t bytes = f * 4 + (size_t)nbins * 2 + R;
-    return (bytes + 15) / 16 * 16;
+__host__ __device__ __forceinline__ size_t smem_bytes_for(uint32_t M, uint32_t G, uint32_t R, uint32_t nbins) {
+    size_t b = (size_t)M * G * 16;                          /* inv_st64 + kq      */
+    b += ((size_t)M * G * 4 + (size_t)M * G * G + (size_t)M * G + 2 * G + (R + 1) + 3 * (size_t)R) * 4;
+    b += (size_t)nbins * 2 + R;
+    return (b + 15) / 16 * 16;
 }
 
 constexpr int WARPS_MAX = 8;        /* blocks of at most 256 threads          */
 constexpr uint32_t CHUNK = 64;      /* particles a warp claims per atomic     */
-constexpr uint32_t STAGE = 64;      /* survivors a warp stages before a flush */
+constexpr uint32_t STAGE = 64;      /* records a warp stages before a flush   */
 
 struct Stage {
     float x[STAGE], mu[STAGE];
     unsigned long long rng[STAGE];
     uint32_t id[STAGE], pk[STAGE];
+    uint4 site[STAGE];
 };
 
-/* flush the first `n` staged survivors of warp w to the out queue (warp-wide) */
-__device__ __forceinline__ void flush_stage(const EvArgs& a, Stage& sg, uint32_t n, int pass, int qout,
-                                            uint32_t lane) {
+/* flush the first n staged survivors of a warp to the out queue (warp-wide) */
+__device__ __forceinline__ void flush_particles(const EvArgs& a, Stage& sg, uint32_t n, int pass, int qout,
+                                                uint32_t lane) {
     unsigned long long base = 0;
     if (lane == 0) base = atomicAdd(&a.qcount[pass], (unsigned long long)n);
     base = __shfl_sync(0xffffffffu, base, 0);
@@ -287,13 +198,38 @@ __device__ __forceinline__ void flush_stage(const EvArgs& a, Stage& sg, uint32_t
     }
 }
 
+/* flush the first n staged sites of a warp into its slab (warp-wide);
+   returns false (all lanes) if the slab is full */
+__device__ __forceinline__ bool flush_sites(const EvArgs& a, Stage& sg, uint32_t n, uint32_t slab,
+                                            uint32_t lane) {
+    unsigned long long base = 0;
+    if (lane == 0) base = atomicAdd(&a.slab_count[slab], (unsigned long long)n);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (base + n > a.slab_cap) return false;
+    for (uint32_t i = lane; i < n; i += 32) a.sites[(uint64_t)slab * a.slab_cap + base + i] = sg.site[i];
+    return true;
+}
+
+__device__ __forceinline__ void move_down(Stage& sg, uint32_t from, uint32_t n, uint32_t lane, bool sites) {
+    /* entries [from, from+n) -> [0, n), n <= 32 */
+    if (sites) {
+        uint4 v = make_uint4(0, 0, 0, 0);
+        if (lane < n) v = sg.site[from + lane];
+        __syncwarp();
+        if (lane < n) sg.site[lane] = v;
+    } else {
+        float x = 0.f, mu = 0.f; unsigned long long r = 0; uint32_t id = 0, pk = 0;
+        if (lane < n) { x = sg.x[from + lane]; mu = sg.mu[from + lane]; r = sg.rng[from + lane]; id = sg.id[from + lane]; pk = sg.pk[from + lane]; }
+        __syncwarp();
+        if (lane < n) { sg.x[lane] = x; sg.mu[lane] = mu; sg.rng[lane] = r; sg.id[lane] = id; sg.pk[lane] = pk; }
+    }
+    __syncwarp();
+}
+
 /*
- * One queue pass.  Each warp works on its own: it claims input particles 64
- * at a time (one global atomic), hands them to idle lanes, advances every
- * live particle by one real collision per iteration, and stages particles
- * that completed K collisions in shared memory, flushing 32 at a time to the
- * output queue with one atomic.  Lanes whose particle dies take the next
- * input particle, so the warp stays full until the input runs out.
+ * One queue pass.  Every warp: claim input particles, give them to idle
+ * lanes, fly every live lane once per iteration, process real collisions,
+ * stage fission sites and particles that completed K real collisions.
  */
 template <bool SOURCE, bool ONE, bool EXACT, bool BANK, bool REC>
 __global__ void __launch_bounds__(256, 3) ev_pass(EvArgs a, int pass, uint32_t K) {
@@ -303,7 +239,9 @@ __global__ void __launch_bounds__(256, 3) ev_pass(EvArgs a, int pass, uint32_t K
     if (ONE) {
         const EvInst& I = a.inst[0];
         const uint32_t M = I.M, G = I.G, R = I.R, NB = I.nbins;
-        float* f = reinterpret_cast<float*>(smem);
+        double* s_inv64 = reinterpret_cast<double*>(smem);
+        unsigned long long* s_kq = reinterpret_cast<unsigned long long*>(s_inv64 + M * G);
+        float* f = reinterpret_cast<float*>(s_kq + M * G);
         float* s_xs = f;                 f += M * G * 4;
         float* s_scdf = f;               f += M * G * G;
         float* s_chi = f;                f += M * G;
@@ -314,6 +252,7 @@ __global__ void __launch_bounds__(256, 3) ev_pass(EvArgs a, int pass, uint32_t K
         uint32_t* s_ncell = reinterpret_cast<uint32_t*>(f);  f += R;
         uint16_t* s_grid = reinterpret_cast<uint16_t*>(f);
         uint8_t* s_rmat = reinterpret_cast<uint8_t*>(s_grid + NB);
+        for (uint32_t i = threadIdx.x; i < M * G; i += blockDim.x) { s_inv64[i] = I.inv_st64[i]; s_kq[i] = I.kq[i]; }
         for (uint32_t i = threadIdx.x; i < M * G * 4; i += blockDim.x) s_xs[i] = I.xs[i];
         for (uint32_t i = threadIdx.x; i < M * G * G; i += blockDim.x) s_scdf[i] = I.scdf[i];
         for (uint32_t i = threadIdx.x; i < M * G; i += blockDim.x) s_chi[i] = I.chicdf[i];
@@ -325,20 +264,24 @@ __global__ void __launch_bounds__(256, 3) ev_pass(EvArgs a, int pass, uint32_t K
         for (uint32_t i = threadIdx.x; i < NB; i += blockDim.x) s_grid[i] = I.grid[i];
         for (uint32_t i = threadIdx.x; i < R; i += blockDim.x) s_rmat[i] = I.rmat[i];
         __syncthreads();
-        t.xs = s_xs; t.scdf = s_scdf; t.chi = s_chi; t.maj = s_maj; t.left = s_left;
-        t.grid = s_grid; t.rmat = s_rmat; t.invdx = s_invdx; t.first = s_first; t.ncell = s_ncell;
+        t.xs = s_xs; t.inv_st64 = s_inv64; t.kq = s_kq; t.scdf = s_scdf; t.chi = s_chi; t.maj = s_maj;
+        t.left = s_left; t.grid = s_grid; t.rmat = s_rmat; t.invdx = s_invdx; t.first = s_first;
+        t.ncell = s_ncell;
         t.G = G; t.R = R; t.nbins = NB; t.L = I.L; t.inv_binw = I.inv_binw;
         t.boundl = I.boundl; t.boundr = I.boundr;
     }
     const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const unsigned lt = (1u << lane) - 1u;
+    const unsigned FULL = 0xffffffffu;
     Stage& sg = s_stage[w];
     const int qin = (pass - 1) & 1, qout = pass & 1;
     const uint64_t n_in = SOURCE ? a.n_total : a.qcount[pass - 1];
     unsigned long long* claim = &a.claim[pass];
-    uint64_t pool_next = 0, pool_end = 0;     /* warp-uniform claimed range */
+    const uint32_t slab = (blockIdx.x * WARPS_MAX + w) % NSLAB;
+    uint64_t pool_next = 0, pool_end = 0;   /* warp-uniform claimed range     */
     bool exhausted = false;
-    uint32_t staged = 0;                      /* warp-uniform               */
+    uint32_t staged = 0, staged_sites = 0;  /* warp-uniform                   */
+    bool slab_full = false;
     Acc acc = {0, 0, 0, 0, 0, 0};
     bool have = false;
     Part p;
@@ -348,9 +291,10 @@ __global__ void __launch_bounds__(256, 3) ev_pass(EvArgs a, int pass, uint32_t K
     TView tv = t;
     float inv_k = 0.0f;
     unsigned long long kq_part = 0;
+    uint32_t draws = 0;
     for (;;) {
-        /* hand input particles to idle lanes */
-        unsigned need = __ballot_sync(0xffffffffu, !have);
+        /* ---- hand input particles to idle lanes ---------------------------- */
+        unsigned need = __ballot_sync(FULL, !have);
         if (need && !exhausted) {
             uint32_t n_need = __popc(need);
             uint64_t avail = pool_end - pool_next;
@@ -358,7 +302,7 @@ __global__ void __launch_bounds__(256, 3) ev_pass(EvArgs a, int pass, uint32_t K
             if (avail < n_need) {
                 unsigned long long base = 0;
                 if (lane == 0) base = atomicAdd(claim, (unsigned long long)CHUNK);
-                base = __shfl_sync(0xffffffffu, base, 0);
+                base = __shfl_sync(FULL, base, 0);
                 if (base < n_in) { nb = base; ne = base + CHUNK < n_in ? base + CHUNK : n_in; }
                 else exhausted = true;
             }
@@ -369,10 +313,8 @@ __global__ void __launch_bounds__(256, 3) ev_pass(EvArgs a, int pass, uint32_t K
                 if (rank < avail) { idx = pool_next + rank; got = true; }
                 else if (rank - avail < ne - nb) { idx = nb + (rank - avail); got = true; }
             }
-            uint64_t take = n_need;
-            if (take <= avail) pool_next += take;
-            else { uint64_t from_new = take - avail; pool_next = nb + from_new; pool_end = ne;
-                   if (pool_next > pool_end) pool_next = pool_end; }
+            if ((uint64_t)n_need <= avail) pool_next += n_need;
+            else { pool_next = nb + (n_need - avail); pool_end = ne; if (pool_next > pool_end) pool_next = pool_end; }
             if (got) {
                 if (SOURCE) {
                     uint32_t inst = 0;
@@ -403,7 +345,7 @@ __global__ void __launch_bounds__(256, 3) ev_pass(EvArgs a, int pass, uint32_t K
                         float sub = u24(nr_pcg32_next(&p.rng));
                         p.x = __fadd_rn(I.cleft[cell], __fmul_rn(sub, I.cdx[cell]));
                         p.mu = __fsub_rn(__fmul_rn(2.0f, u24(nr_pcg32_next(&p.rng))), 1.0f);
-                        p.g = chi_group(I.chicdf + (uint32_t)I.cmat[cell] * I.G, I.G, u24(nr_pcg32_next(&p.rng)));
+                        p.g = count_below(I.chicdf + (uint32_t)I.cmat[cell] * I.G, I.G, u24(nr_pcg32_next(&p.rng)));
                     }
                     if (REC && inst == 0) a.rec[p.local].draws += (nbk > 0) ? 1 : 4;
                 } else {
@@ -428,17 +370,121 @@ __global__ void __launch_bounds__(256, 3) ev_pass(EvArgs a, int pass, uint32_t K
                 kq_part = 0;
             }
         }
-        if (!__any_sync(0xffffffffu, have)) break;
+        if (!__any_sync(FULL, have)) break;
+
+        /* ---- one flight per live lane --------------------------------------- */
+        const uint32_t G = tv.G;
+        nraps_history_record* rec = (REC && have && p.inst == 0) ? &a.rec[p.local] : nullptr;
+        if (REC) draws = 0;
+        auto next = [&]() -> uint32_t { if (REC) ++draws; return nr_pcg32_next(&p.rng); };
+        int fate = -1;
+        bool real = false;
+        uint32_t m = 0, cell = 0, pending = 0;
+        if (have) {
+            if (++events > a.max_events) {
+                fate = NRAPS_FATE_CAPPED;
+            } else {
+                float d = __fmul_rn(neg_log<EXACT>(u24pos(next())), tv.maj[G + p.g]);
+                p.x = __fadd_rn(p.x, __fmul_rn(p.mu, d));
+                int bounce = 0;
+                while (!(p.x >= 0.0f && p.x <= tv.L)) {
+                    if (p.x > tv.L) {
+                        if (tv.boundr > 0.0f) { p.x = __fsub_rn(tv.L, __fsub_rn(p.x, tv.L)); p.mu = -p.mu; }
+                        else { fate = NRAPS_FATE_LEAKED; break; }
+                    } else {
+                        if (tv.boundl > 0.0f) { p.x = -p.x; p.mu = -p.mu; }
+                        else { fate = NRAPS_FATE_LEAKED; break; }
+                    }
+                    if (++bounce > 1000) { fate = NRAPS_FATE_CAPPED; break; }
+                }
+                if (fate < 0) {
+                    uint32_t r = region_of(tv, p.x);
+                    m = tv.rmat[r];
+                    if (__fmul_rn(u24(next()), tv.maj[p.g]) < tv.xs[(m * G + p.g) * 4]) {
+                        real = true;
+                        acc.coll++;
+                        float rel = __fmul_rn(__fsub_rn(p.x, tv.left[r]), tv.invdx[r]);
+                        uint32_t nr = tv.ncell[r];
+                        uint32_t k = rel > 0.0f ? (uint32_t)rel : 0u;
+                        if (k >= nr) k = nr - 1;
+                        cell = tv.first[r] + k;
+                        const uint32_t j = m * G + p.g;
+                        atomicAdd(&Ip->tally[(uint64_t)p.g * Ip->nc + cell], tv.inv_st64[j]);
+                        unsigned long long q = tv.kq[j];
+                        acc.kq += q;
+                        kq_part += q;
+                        if (REC && rec) {
+                            rec->collisions++;
+                            rec->track += tv.inv_st64[j];
+                            rec->nsf_track += (double)tv.xs[j * 4 + 2];
+                            rec->final_cell = cell;
+                        }
+                        if (BANK) {
+                            float nu = __fadd_rn(__fmul_rn(tv.xs[j * 4 + 2], inv_k), u24(next()));
+                            int n = (int)floorf(nu);
+                            pending = n > 64 ? 64u : (uint32_t)n;
+                        }
+                    } else {
+                        acc.virt++;
+                        if (REC && rec) rec->crossings++;
+                    }
+                }
+            }
+        }
+        /* ---- fission sites: one per pending lane per round ------------------ */
+        if (BANK) {
+            while (__any_sync(FULL, pending > 0)) {
+                unsigned sm = __ballot_sync(FULL, pending > 0);
+                if (pending > 0) {
+                    uint32_t sgp = count_below(tv.chi + m * G, G, u24(next()));
+                    uint32_t slot = staged_sites + __popc(sm & lt);
+                    sg.site[slot] = make_uint4(__float_as_uint(p.x), cell | (sgp << 27), p.id,
+                                               (p.seq & 0xFFFFu) | (p.inst << 16));
+                    if (p.seq >= 0xFFFFu) atomicOr(&Ip->st->error, NR_ERR_CAPACITY);
+                    p.seq++;
+                    pending--;
+                }
+                staged_sites += __popc(sm);
+                __syncwarp();
+                if (staged_sites >= 32) {
+                    if (!flush_sites(a, sg, 32, slab, lane)) slab_full = true;
+                    move_down(sg, 32, staged_sites - 32, lane, true);
+                    staged_sites -= 32;
+                }
+            }
+        }
+        /* ---- absorb or scatter ------------------------------------------------ */
         bool push = false;
         if (have) {
-            int f = step_particle<EXACT, BANK, REC>(a, *Ip, tv, p, inv_k, acc, events, kq_part);
-            ++done;
-            if (f != 0) have = false;
-            else if (done >= K) { push = true; have = false; }
+            if (real) {
+                const uint32_t j = m * G + p.g;
+                if (u24(next()) < tv.xs[j * 4 + 1]) {
+                    fate = NRAPS_FATE_ABSORBED;
+                } else {
+                    p.g = count_le(tv.scdf + j * G, G, u24(next()));
+                    p.mu = __fsub_rn(__fmul_rn(2.0f, u24(next())), 1.0f);
+                }
+                ++done;
+            }
+            if (REC && rec) rec->draws += draws;
+            if (fate >= 0) {
+                if (fate == NRAPS_FATE_ABSORBED) acc.absorbed++;
+                else if (fate == NRAPS_FATE_LEAKED) acc.leaked++;
+                else { acc.capped++; atomicOr(&Ip->st->error, NR_ERR_CAPPED); }
+                if (BANK) a.count[p.id] = p.seq;
+                if (REC && rec) {
+                    rec->fate = fate; rec->final_group = p.g; rec->final_x = (double)p.x;
+                    rec->n_sites = p.seq;
+                }
+                have = false;
+            } else if (real && done >= K) {
+                push = true;
+                have = false;
+            }
             if (!have && !ONE && kq_part) { atomicAdd(&Ip->st->kq, kq_part); kq_part = 0; }
         }
-        /* stage survivors; flush 32 at a time */
-        unsigned pm = __ballot_sync(0xffffffffu, push);
+        /* ---- stage survivors; flush 32 at a time ------------------------------ */
+        unsigned pm = __ballot_sync(FULL, push);
         if (pm) {
             if (push) {
                 uint32_t slot = staged + __popc(pm & lt);
@@ -448,26 +494,18 @@ __global__ void __launch_bounds__(256, 3) ev_pass(EvArgs a, int pass, uint32_t K
             staged += __popc(pm);
             __syncwarp();
             if (staged >= 32) {
-                flush_stage(a, sg, 32, pass, qout, lane);
+                flush_particles(a, sg, 32, pass, qout, lane);
                 __syncwarp();
-                uint32_t rest = staged - 32;
-                float x2 = 0.f, mu2 = 0.f; unsigned long long r2 = 0; uint32_t id2 = 0, pk2 = 0;
-                if (lane < rest) {
-                    x2 = sg.x[32 + lane]; mu2 = sg.mu[32 + lane]; r2 = sg.rng[32 + lane];
-                    id2 = sg.id[32 + lane]; pk2 = sg.pk[32 + lane];
-                }
-                __syncwarp();
-                if (lane < rest) { sg.x[lane] = x2; sg.mu[lane] = mu2; sg.rng[lane] = r2; sg.id[lane] = id2; sg.pk[lane] = pk2; }
-                __syncwarp();
-                staged = rest;
+                move_down(sg, 32, staged - 32, lane, false);
+                staged -= 32;
             }
         }
     }
-    if (staged) {
-        __syncwarp();
-        flush_stage(a, sg, staged, pass, qout, lane);
-    }
-    /* flush counters: one atomic per warp */
+    __syncwarp();
+    if (staged) flush_particles(a, sg, staged, pass, qout, lane);
+    if (BANK && staged_sites) { if (!flush_sites(a, sg, staged_sites, slab, lane)) slab_full = true; }
+    if (slab_full && lane == 0) atomicOr(&a.inst[0].st->error, NR_ERR_CAPACITY);
+    /* ---- counters: one atomic per warp ---------------------------------------- */
     unsigned long long kq = nrdev::warp_sum_u64(ONE ? acc.kq : 0ull);
     unsigned long long coll = nrdev::warp_sum_u64(acc.coll), virt = nrdev::warp_sum_u64(acc.virt);
     unsigned long long ab = nrdev::warp_sum_u64(acc.absorbed), lk = nrdev::warp_sum_u64(acc.leaked);
@@ -492,27 +530,50 @@ __device__ __forceinline__ uint32_t find_inst(const uint64_t* begin, uint32_t n,
     return lo;
 }
 
-/* ordered bank: site (parent, seq) -> offsets[parent] + seq - offsets[first history of its instance] */
-__global__ void ev_scatter(EvArgs a) {
+/* ordered bank: site (parent, seq) -> offsets[parent] + seq - offsets[first
+   history of its instance]; blocks walk the filled part of one slab each */
+template <bool ONE>
+__global__ void __launch_bounds__(256) ev_scatter(EvArgs a) {
     const uint32_t slab = blockIdx.x % NSLAB;
     const uint64_t per = gridDim.x / NSLAB;
     uint64_t filled = a.slab_count[slab];
     if (filled > a.slab_cap) filled = a.slab_cap;
+    const uint4* src = a.sites + (uint64_t)slab * a.slab_cap;
+    /* single instance: its descriptor fields once per thread */
+    nraps_site* out0 = nullptr;
+    uint64_t cap0 = 0;
+    uint32_t* hist0 = nullptr;
+    if (ONE) {
+        const EvInst& I = a.inst[0];
+        out0 = I.bank[(I.st->gen + 1) & 1];
+        cap0 = I.bank_cap;
+        hist0 = I.hist;
+    }
     for (uint64_t j = (uint64_t)(blockIdx.x / NSLAB) * blockDim.x + threadIdx.x; j < filled;
          j += per * blockDim.x) {
-        uint64_t i = (uint64_t)slab * a.slab_cap + j;
-        uint32_t gi = a.sgi[i];
-        uint32_t inst = gi >> 4;
-        const EvInst& I = a.inst[inst];
-        uint64_t pos = (uint64_t)a.offsets[a.sparent[i]] + a.sseq[i] - a.offsets[I.hist_begin];
-        if (pos < I.bank_cap) {
-            nraps_site s;
-            s.x = a.sx[i];
-            s.cell = a.scell[i];
-            s.group = gi & 15u;
-            s.pad = 0;
-            I.bank[(I.st->gen + 1) & 1][pos] = s;
-            atomicAdd(&I.hist[(uint64_t)s.cell * HIST_STRIDE], 1u);
+        uint4 v = src[j];
+        uint32_t inst = v.w >> 16;
+        /* a slab that overflowed keeps stale records: never follow them */
+        if (v.z >= a.n_total || inst >= a.n_inst) continue;
+        uint32_t cell = v.y & 0x07FFFFFFu;
+        nraps_site s;
+        s.x = __uint_as_float(v.x);
+        s.cell = cell;
+        s.group = v.y >> 27;
+        s.pad = 0;
+        if (ONE) {
+            uint64_t pos = (uint64_t)a.offsets[v.z] + (v.w & 0xFFFFu);
+            if (pos < cap0) {
+                out0[pos] = s;
+                atomicAdd(&hist0[(uint64_t)cell * HIST_STRIDE], 1u);
+            }
+        } else {
+            const EvInst& I = a.inst[inst];
+            uint64_t pos = (uint64_t)a.offsets[v.z] + (v.w & 0xFFFFu) - a.offsets[I.hist_begin];
+            if (pos < I.bank_cap) {
+                I.bank[(I.st->gen + 1) & 1][pos] = s;
+                atomicAdd(&I.hist[(uint64_t)cell * HIST_STRIDE], 1u);
+            }
         }
     }
 }
@@ -525,6 +586,7 @@ __device__ void finish_instance(const EvArgs& a, uint32_t i) {
     if (gen >= I.generations) return;
     double k_new = nr_unfix(st->kq) / (double)I.N;
     I.k64[gen] = k_new;
+    if (gen >= I.skip) { st->ksum += k_new; st->ksum2 += k_new * k_new; st->nactive++; }
     I.entropy[gen] = a.bank ? st->h_acc : 0.0;
     if (a.bank) {
         unsigned long long B = a.offsets[I.hist_begin + I.N] - a.offsets[I.hist_begin];
@@ -547,13 +609,17 @@ __device__ void finish_instance(const EvArgs& a, uint32_t i) {
     st->gen = gen + 1;
 }
 
+constexpr int FIN_THREADS = 64;
+
 /*
  * One thread per (instance, cell): reads and clears the cell's G tally bins,
- * accumulates flux and fission source of active generations, and the cell's
- * entropy term.  The last block to finish (threadfence + counter, no waiting)
- * then closes the generation of every instance and resets the pass counters.
+ * accumulates flux and fission source of active generations (multiplications
+ * by precomputed reciprocals: FP64 division is slow on this part), and the
+ * cell's entropy term.  The last block to finish (threadfence + counter, no
+ * waiting) then closes the generation of every instance and resets the pass
+ * counters.
  */
-__global__ void __launch_bounds__(256) ev_finalize(EvArgs a) {
+__global__ void __launch_bounds__(FIN_THREADS) ev_finalize(EvArgs a) {
     __shared__ bool s_last;
     for (uint64_t gc0 = (uint64_t)blockIdx.x * blockDim.x; gc0 < a.n_cells_total;
          gc0 += (uint64_t)gridDim.x * blockDim.x) {
@@ -570,20 +636,19 @@ __global__ void __launch_bounds__(256) ev_finalize(EvArgs a) {
                 const bool active = gen >= I.skip;
                 const double fund = 1.0 / (double)(I.generations - I.skip);
                 const double k = st->k;
-                const double conversion = I.conv_const * k;
-                const double N = (double)I.N;
-                double dx = I.dx64[c];
+                const double phi_scale = I.inv_dx64[c] / (double)I.N;   /* 1/(N dx)   */
+                const double flux_scale = phi_scale / k;                /* 1/(k N dx) */
+                const double acc_scale = flux_scale * (I.conv_const * k) * fund;
                 uint32_t m = I.cmat[c];
                 double fs = 0.0;
                 for (uint32_t g = 0; g < I.G; ++g) {
                     uint64_t bin = (uint64_t)g * I.nc + c;
                     double tl = I.tally[bin];
                     I.tally[bin] = 0.0;
-                    double flux = tl / (k * N * dx);
-                    fs += I.nsf64[m + (uint64_t)I.M * g] * flux;
-                    double phi = tl / (N * dx);
+                    fs += I.nsf64[m + (uint64_t)I.M * g] * (tl * flux_scale);
                     if (active) {
-                        I.flux_acc[bin] += flux * conversion * fund;
+                        double phi = tl * phi_scale;
+                        I.flux_acc[bin] += tl * acc_scale;
                         I.flux_sum[bin] += phi;
                         I.flux_sq[bin] += phi * phi;
                     }
@@ -640,6 +705,9 @@ __global__ void __launch_bounds__(256) ev_finalize(EvArgs a) {
 template <class T> struct DBuf {
     T* p = nullptr;
     size_t n = 0;
+    DBuf() = default;
+    DBuf(const DBuf&) = delete;
+    DBuf& operator=(const DBuf&) = delete;
     ~DBuf() { if (p) cudaFree(p); }
     cudaError_t alloc(size_t count) {
         if (p) { cudaFree(p); p = nullptr; }
@@ -667,10 +735,10 @@ struct EventEngine::Impl {
     DBuf<unsigned long long> qrng[2];
     DBuf<uint32_t> qid[2], qpk[2];
     DBuf<unsigned long long> qcount, slab_count;
-    DBuf<float> sx;
-    DBuf<uint32_t> scell, sgi, sparent, sseq, count, offsets, block_sums;
+    DBuf<uint4> sites;
+    DBuf<uint32_t> count, offsets, block_sums;
     DBuf<GenState> bstats;
-    uint64_t n_total = 0, n_cells_total = 0, slab_cap = 0;
+    uint64_t n_total = 0, n_cells_total = 0, slab_cap = 0, cap_total = 0, cap_inst = 0;
     nraps_history_record* rec = nullptr;
     EvArgs args{};
     bool committed = false;
@@ -700,8 +768,8 @@ int EventEngine::configure(const nraps_opts& o, std::string& err) {
 
 uint64_t EventEngine::table_bytes(const nraps_problem& p) {
     uint64_t M = p.variables.mattypes, G = p.variables.energygroups, nc = p.mesh.n_cells;
-    return (M * G * (4 + G + 1) + 2 * G) * 4 + nc * (4 + 4 + 1 + 8) + M * G * 8 + p.n_fuel * 4 +
-           nc * (4 + 4 + 4 + 4 + 1) + 16384 * 2 + 16 * 256;
+    return (M * G * (4 + G + 1) + 2 * G) * 4 + M * G * 16 + M * G * 8 + p.n_fuel * 4 +
+           nc * (4 + 4 + 1 + 8) + nc * (4 + 4 + 4 + 4 + 1) + 16384 * 2 + 20 * 256;
 }
 
 int EventEngine::add_instance(const nraps_problem& p, const EvBuffers& b, std::string& err) {
@@ -711,33 +779,38 @@ int EventEngine::add_instance(const nraps_problem& p, const EvBuffers& b, std::s
     const EvHostTables& h = in->h;
     size_t off = 0;
     auto take = [&](size_t bytes) { size_t o = off; off = (off + bytes + 255) & ~(size_t)255; return o; };
-    size_t o_xs = take(h.xs.size() * 4), o_scdf = take(h.scdf.size() * 4), o_chi = take(h.chicdf.size() * 4);
+    size_t o_xs = take(h.xs.size() * 4), o_inv64 = take(h.inv_st64.size() * 8), o_kq = take(h.kq.size() * 8);
+    size_t o_scdf = take(h.scdf.size() * 4), o_chi = take(h.chicdf.size() * 4);
     size_t o_maj = take(h.maj.size() * 4), o_left = take(h.rleft.size() * 4), o_invdx = take(h.rinvdx.size() * 4);
     size_t o_rmat = take(h.rmat.size()), o_rfirst = take(h.rfirst.size() * 4), o_rn = take(h.rncell.size() * 4);
     size_t o_grid = take(h.grid.size() * 2), o_fuel = take(h.fuel.size() * 4), o_cleft = take(h.cleft.size() * 4);
     size_t o_cdx = take(h.cdx.size() * 4), o_cmat = take(h.cmat.size()), o_nsf = take(h.nsf64.size() * 8);
-    size_t o_dx = take(h.dx64.size() * 8);
+    size_t o_idx = take(h.inv_dx64.size() * 8);
     std::vector<unsigned char> host(off, 0);
     auto put = [&](size_t o, const void* src, size_t bytes) { if (bytes) std::memcpy(host.data() + o, src, bytes); };
-    put(o_xs, h.xs.data(), h.xs.size() * 4); put(o_scdf, h.scdf.data(), h.scdf.size() * 4);
+    put(o_xs, h.xs.data(), h.xs.size() * 4); put(o_inv64, h.inv_st64.data(), h.inv_st64.size() * 8);
+    put(o_kq, h.kq.data(), h.kq.size() * 8);
+    put(o_scdf, h.scdf.data(), h.scdf.size() * 4);
     put(o_chi, h.chicdf.data(), h.chicdf.size() * 4); put(o_maj, h.maj.data(), h.maj.size() * 4);
     put(o_left, h.rleft.data(), h.rleft.size() * 4); put(o_invdx, h.rinvdx.data(), h.rinvdx.size() * 4);
     put(o_rmat, h.rmat.data(), h.rmat.size()); put(o_rfirst, h.rfirst.data(), h.rfirst.size() * 4);
     put(o_rn, h.rncell.data(), h.rncell.size() * 4); put(o_grid, h.grid.data(), h.grid.size() * 2);
     put(o_fuel, h.fuel.data(), h.fuel.size() * 4); put(o_cleft, h.cleft.data(), h.cleft.size() * 4);
     put(o_cdx, h.cdx.data(), h.cdx.size() * 4); put(o_cmat, h.cmat.data(), h.cmat.size());
-    put(o_nsf, h.nsf64.data(), h.nsf64.size() * 8); put(o_dx, h.dx64.data(), h.dx64.size() * 8);
+    put(o_nsf, h.nsf64.data(), h.nsf64.size() * 8); put(o_idx, h.inv_dx64.data(), h.inv_dx64.size() * 8);
     cudaError_t e = in->blob.alloc(off);
     if (e == cudaSuccess) e = cudaMemcpy(in->blob.p, host.data(), off, cudaMemcpyHostToDevice);
     if (e != cudaSuccess) { err = std::string("event tables: ") + cudaGetErrorString(e); delete in; return -1; }
     unsigned char* B = in->blob.p;
     EvInst& d = in->d;
-    d.xs = (const float*)(B + o_xs); d.scdf = (const float*)(B + o_scdf); d.chicdf = (const float*)(B + o_chi);
+    d.xs = (const float*)(B + o_xs); d.inv_st64 = (const double*)(B + o_inv64);
+    d.kq = (const unsigned long long*)(B + o_kq);
+    d.scdf = (const float*)(B + o_scdf); d.chicdf = (const float*)(B + o_chi);
     d.maj = (const float*)(B + o_maj); d.rleft = (const float*)(B + o_left); d.rinvdx = (const float*)(B + o_invdx);
     d.rmat = B + o_rmat; d.rfirst = (const uint32_t*)(B + o_rfirst); d.rncell = (const uint32_t*)(B + o_rn);
     d.grid = (const uint16_t*)(B + o_grid); d.fuel = (const uint32_t*)(B + o_fuel);
     d.cleft = (const float*)(B + o_cleft); d.cdx = (const float*)(B + o_cdx); d.cmat = B + o_cmat;
-    d.nsf64 = (const double*)(B + o_nsf); d.dx64 = (const double*)(B + o_dx);
+    d.nsf64 = (const double*)(B + o_nsf); d.inv_dx64 = (const double*)(B + o_idx);
     d.M = h.M; d.G = h.G; d.R = h.R; d.nc = h.nc; d.nbins = h.nbins; d.nfuel = h.nfuel;
     d.L = h.L; d.inv_binw = h.inv_binw; d.boundl = h.boundl; d.boundr = h.boundr;
     d.N = p.variables.histories; d.seed = b.seed;
@@ -750,6 +823,13 @@ int EventEngine::add_instance(const nraps_problem& p, const EvBuffers& b, std::s
     impl_->inst.push_back(in);
     impl_->committed = false;
     return (int)impl_->inst.size() - 1;
+}
+
+void EventEngine::remove_instance(uint32_t idx) {
+    if (idx >= impl_->inst.size()) return;
+    delete impl_->inst[idx];
+    impl_->inst.erase(impl_->inst.begin() + idx);
+    impl_->committed = false;
 }
 
 void EventEngine::clear_instances() {
@@ -766,13 +846,13 @@ GenState* EventEngine::batch_stats() const { return impl_->bstats.p; }
 
 uint64_t EventEngine::shared_bytes() const {
     const Impl* m = impl_;
-    return m->n_total * (24 * 2 + 8) + NSLAB * m->slab_cap * 20;
+    return m->n_total * (24 * 2 + 8) + NSLAB * m->slab_cap * 16;
 }
 
 namespace {
 template <bool SOURCE, bool ONE, bool EXACT, bool BANK, bool REC>
 void set_smem_attr(size_t smem) {
-    static size_t granted = 48 * 1024;          /* default dynamic limit */
+    static size_t granted = 16 * 1024;          /* below the default dynamic limit */
     if (smem > granted) {
         cudaFuncSetAttribute(ev_pass<SOURCE, ONE, EXACT, BANK, REC>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -814,7 +894,6 @@ int EventEngine::commit(cudaStream_t s, std::string& err) {
     }
     if (ib[n] >= (1ULL << 32)) { err = "at most 2^32-1 particles per batch generation"; return NRAPS_ERR_INVALID; }
     bool bank = m.mode == NRAPS_MODE_BANK;
-    uint64_t old_total = m.n_total;
     m.n_total = ib[n];
     m.n_cells_total = cb[n];
     std::vector<EvInst> d(n);
@@ -822,30 +901,36 @@ int EventEngine::commit(cudaStream_t s, std::string& err) {
     for (uint32_t i = 0; i < n; ++i) { d[i] = m.inst[i]->d; bank_sum += m.inst[i]->b.bank_cap; }
     cudaError_t e = cudaSuccess;
     auto A = [&](cudaError_t x) { if (e == cudaSuccess) e = x; };
-    if (m.d_inst.n < n) A(m.d_inst.alloc(n));
-    if (m.d_inst_begin.n < n + 1) { A(m.d_inst_begin.alloc(n + 1)); A(m.d_cell_begin.alloc(n + 1)); }
+    /* shared buffers grow geometrically, so a batch whose membership changes
+       between generations reallocates rarely */
+    if (m.cap_inst < n) {
+        m.cap_inst = std::max<uint64_t>(n, m.cap_inst + m.cap_inst / 2);
+        A(m.d_inst.alloc(m.cap_inst)); A(m.d_inst_begin.alloc(m.cap_inst + 1)); A(m.d_cell_begin.alloc(m.cap_inst + 1));
+    }
     A(cudaMemcpyAsync(m.d_inst.p, d.data(), n * sizeof(EvInst), cudaMemcpyHostToDevice, s));
     A(cudaMemcpyAsync(m.d_inst_begin.p, ib.data(), (n + 1) * 8, cudaMemcpyHostToDevice, s));
     A(cudaMemcpyAsync(m.d_cell_begin.p, cb.data(), (n + 1) * 8, cudaMemcpyHostToDevice, s));
-    if (m.n_total > old_total || !m.qx[0].p) {
+    if (m.n_total > m.cap_total || !m.qx[0].p) {
+        m.cap_total = std::max<uint64_t>(m.n_total, m.cap_total + m.cap_total / 2);
+        uint64_t c = m.cap_total;
         for (int q = 0; q < 2; ++q) {
-            A(m.qx[q].alloc(m.n_total)); A(m.qmu[q].alloc(m.n_total)); A(m.qrng[q].alloc(m.n_total));
-            A(m.qid[q].alloc(m.n_total)); A(m.qpk[q].alloc(m.n_total));
+            A(m.qx[q].alloc(c)); A(m.qmu[q].alloc(c)); A(m.qrng[q].alloc(c));
+            A(m.qid[q].alloc(c)); A(m.qpk[q].alloc(c));
         }
-        A(m.count.alloc(m.n_total)); A(m.offsets.alloc(m.n_total + 1));
-        A(m.block_sums.alloc((m.n_total + 4095) / 4096 + 1));
+        A(m.count.alloc(c)); A(m.offsets.alloc(c + 1));
+        A(m.block_sums.alloc((c + 4095) / 4096 + 1));
     }
     if (!m.qcount.p) { A(m.qcount.alloc(2 * (MAX_PASSES + 2) + 2)); A(m.slab_count.alloc(NSLAB)); A(m.bstats.alloc(1)); }
-    uint64_t want_slab = bank ? (bank_sum + 2 * m.n_total) / NSLAB + 4096 : 1;
-    if (want_slab > m.slab_cap || !m.sx.p) {
-        m.slab_cap = want_slab;
-        uint64_t tot = NSLAB * m.slab_cap;
-        A(m.sx.alloc(tot)); A(m.scell.alloc(tot)); A(m.sgi.alloc(tot)); A(m.sparent.alloc(tot)); A(m.sseq.alloc(tot));
+    /* slabs: room for every banked site plus one partial flush per warp */
+    uint64_t want_slab = bank ? (bank_sum + 2 * m.n_total) / NSLAB + 8192 : 64;
+    if (want_slab > m.slab_cap || !m.sites.p) {
+        m.slab_cap = std::max<uint64_t>(want_slab, m.slab_cap + m.slab_cap / 2);
+        A(m.sites.alloc(NSLAB * m.slab_cap));
     }
     A(cudaMemsetAsync(m.qcount.p, 0, (2 * (MAX_PASSES + 2) + 2) * 8, s));
     A(cudaMemsetAsync(m.slab_count.p, 0, NSLAB * 8, s));
     A(cudaMemsetAsync(m.bstats.p, 0, sizeof(GenState), s));
-    if (bank) A(cudaMemsetAsync(m.count.p, 0, m.n_total * 4, s));
+    if (bank && m.n_total) A(cudaMemsetAsync(m.count.p, 0, m.n_total * 4, s));
     if (e != cudaSuccess) { err = std::string("event engine buffers: ") + cudaGetErrorString(e); return NRAPS_ERR_NOMEM; }
     EvArgs& a = m.args;
     a.inst = m.d_inst.p; a.n_inst = n; a.inst_begin = m.d_inst_begin.p; a.cell_begin = m.d_cell_begin.p;
@@ -856,20 +941,20 @@ int EventEngine::commit(cudaStream_t s, std::string& err) {
     a.qcount = m.qcount.p;
     a.claim = m.qcount.p + (MAX_PASSES + 2);
     a.blocks_done = m.qcount.p + 2 * (MAX_PASSES + 2);
-    a.sx = m.sx.p; a.scell = m.scell.p; a.sgi = m.sgi.p; a.sparent = m.sparent.p; a.sseq = m.sseq.p;
+    a.sites = m.sites.p;
     a.slab_count = m.slab_count.p; a.slab_cap = m.slab_cap;
     a.count = m.count.p; a.offsets = m.offsets.p;
     a.stats = (n == 1) ? m.inst[0]->d.st : m.bstats.p;
     a.max_events = m.max_events;
     a.rec = m.rec;
     a.bank = bank ? 1 : 0;
-    /* one instance with tables that fit: stage them in shared memory */
+    /* one instance whose tables fit: stage them in shared memory */
     m.one = false;
     m.smem_bytes = 0;
     if (n == 1) {
         const EvInst& I = m.inst[0]->d;
-        size_t sb = smem_words(I.M, I.G, I.R, I.nbins);
-        if (sb <= 160 * 1024) { m.one = true; m.smem_bytes = sb; }
+        size_t sb = smem_bytes_for(I.M, I.G, I.R, I.nbins);
+        if (sb <= 120 * 1024) { m.one = true; m.smem_bytes = sb; }
     }
     m.committed = true;
     return size_grid();
@@ -885,7 +970,7 @@ int EventEngine::size_grid() {
     const void* fn = m.one ? (m.exact ? (const void*)ev_pass<false, true, true, true, false>
                                       : (const void*)ev_pass<false, true, false, true, false>)
                            : (const void*)ev_pass<false, false, false, true, false>;
-    if (m.one && m.smem_bytes > 48 * 1024)
+    if (m.one && m.smem_bytes > 16 * 1024)
         cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)m.smem_bytes);
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, (int)params.block,
                                                       m.one ? m.smem_bytes : 0) != cudaSuccess || per_sm < 1)
@@ -893,8 +978,6 @@ int EventEngine::size_grid() {
     m.grid_blocks = sms * per_sm;
     return NRAPS_OK;
 }
-
-
 
 uint64_t EventEngine::launches_per_generation() const { return 1 + params.passes; }
 
@@ -926,12 +1009,14 @@ int EventEngine::enqueue_generation(cudaStream_t s, bool with_finalize, cudaEven
         int q = launch_exclusive_scan(m.count.p, m.n_total, m.block_sums.p, m.offsets.p, nullptr, s);
         if (q < 0) return -1;
         n += q;
-        ev_scatter<<<NSLAB * 8, 256, 0, s>>>(a);
+        if (m.one || rec) ev_scatter<true><<<NSLAB * 8, 256, 0, s>>>(a);
+        else ev_scatter<false><<<NSLAB * 8, 256, 0, s>>>(a);
         ++n;
     }
     if (with_finalize) {
-        unsigned gb = (unsigned)std::min<uint64_t>((m.n_cells_total + 255) / 256, (uint64_t)m.grid_blocks * 2);
-        ev_finalize<<<gb ? gb : 1, 256, 0, s>>>(a);
+        unsigned gb = (unsigned)std::min<uint64_t>((m.n_cells_total + FIN_THREADS - 1) / FIN_THREADS,
+                                                   (uint64_t)m.grid_blocks * 4);
+        ev_finalize<<<gb ? gb : 1, FIN_THREADS, 0, s>>>(a);
         n += 1;
     }
     return cudaPeekAtLastError() == cudaSuccess ? n : -1;

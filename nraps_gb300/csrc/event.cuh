@@ -57,6 +57,8 @@ public:
     /* Build tables for one problem; returns the instance index, or -1. */
     int add_instance(const nraps_problem& p, const EvBuffers& b, std::string& err);
     void clear_instances();
+    /* Drop one instance (later instances shift down by one). */
+    void remove_instance(uint32_t idx);
     uint32_t n_instances() const;
     /* Upload descriptors and size the shared queues/site slabs. */
     int commit(cudaStream_t s, std::string& err);

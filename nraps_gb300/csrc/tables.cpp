@@ -8,6 +8,7 @@
  * cumulative chi follows energy() (src/mc_code.rs:19-30).
  */
 #include "tables.hpp"
+#include "nr_math.h"
 
 #include <algorithm>
 #include <cmath>
@@ -198,7 +199,17 @@ int build_event_tables(const nraps_problem& p, EvHostTables& t, std::string& err
     t.nsf64.resize(M * G);
     for (uint64_t i = 0; i < M * G; ++i) t.nsf64[i] = (double)x.nut[i] * (double)x.sigf[i];
     t.dx64.resize(nc);
-    for (uint64_t c = 0; c < nc; ++c) t.dx64[c] = (double)p.mesh.delta_x[c];
+    t.inv_dx64.resize(nc);
+    for (uint64_t c = 0; c < nc; ++c) {
+        t.dx64[c] = (double)p.mesh.delta_x[c];
+        t.inv_dx64[c] = 1.0 / t.dx64[c];
+    }
+    t.inv_st64.resize(M * G);
+    t.kq.resize(M * G);
+    for (uint64_t j = 0; j < M * G; ++j) {
+        t.inv_st64[j] = (double)t.xs[j * 4 + 3];
+        t.kq[j] = nr_fix((double)t.xs[j * 4 + 2]);
+    }
     uint64_t inu = std::min<uint64_t>(M, M * G - 1);
     t.conv_const = 3565e6 * 36.2 /
         (200e6 * 1.602176634e-19 * (double)x.nut[inu] * (double)p.mesh.mesh_right[nc - 1]);

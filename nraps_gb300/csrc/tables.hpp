@@ -30,7 +30,9 @@ struct EvHostTables {
     std::vector<uint8_t> rmat, cmat;
     std::vector<uint32_t> rfirst, rncell, fuel;
     std::vector<uint16_t> grid;
-    std::vector<double> nsf64, dx64;
+    std::vector<double> nsf64, dx64, inv_dx64;
+    std::vector<double> inv_st64;       /* [m*G+g] (double)(1/sigtr): flux score  */
+    std::vector<uint64_t> kq;           /* [m*G+g] nsf_st in 2^-32 fixed point    */
     double conv_const = 0.0;
 };
 int build_event_tables(const nraps_problem& p, EvHostTables& t, std::string& err);
