@@ -191,6 +191,57 @@ def measure_e2e(prob, arm: str, seed: int, device: int):
                 k_sigma=r.stats.k_sigma)
 
 
+def measure_batched(seed: int, device: int, steps: int, warmup: int = 3):
+    """256 independent slabs (regions U{4..64}, groups U{2..8}, widths
+    U[0.5,3] cm, histories log-uniform [10k,500k]) advancing together, one
+    CUDA-graph replay per generation."""
+    import torch
+    from nraps_gb300 import api, synth
+    probs = synth.batched(seed, n=256, inactive=max(20, warmup), active=max(20, steps))
+    ctx = api.Context(seed=seed, device=device, use_graphs=1, **ARMS["event"])
+    b = api.Batch(ctx, probs, seeds=[seed * 1000 + i for i in range(len(probs))])
+    b.run(warmup)
+    t0 = b.timing()
+    launches0 = ctx.launches
+    b.run(steps)
+    t1 = b.timing()
+    ms = t1["ms"] - t0["ms"]
+    hist = t1["histories"] - t0["histories"]
+    out = {"instances": len(probs), "histories_per_generation": sum(p.histories for p in probs),
+           "steps": steps, "ms_per_step": ms / steps, "histories_per_s": hist / (ms / 1000.0),
+           "collisions_per_s": (t1["collisions"] - t0["collisions"]) / (ms / 1000.0),
+           "gpu_launches": ctx.launches - launches0, "graphs": True,
+           "groups": "U{2..8}", "regions": "U{4..64}"}
+    b.close()
+    ctx.close()
+    return out
+
+
+def measure_serving(seed: int, device: int, seconds: float, rate: float):
+    from nraps_gb300 import api, serving
+    ctx = api.Context(seed=seed, device=device, **ARMS["event"])
+    r = serving.run_poisson(ctx, rate=rate, seconds=seconds, seed=seed)
+    ctx.close()
+    return r
+
+
+def measure_scale_stress(seed: int, device: int):
+    """8 groups, 10,000 regions, 200,000 cells, 10M histories, 20 + 50."""
+    from nraps_gb300 import synth
+    prob = synth.scale_stress(seed)
+    d = measure_device(prob, "event", prob.generations - prob.skip, prob.skip, seed, device)
+    per_launch_ms = d["transport_ms"] / max(1, d["transport_launches"])
+    coll_per_launch = d["collisions"] / max(1, d["transport_launches"])
+    return {"workload": "scale_stress", "cells": prob.n_cells, "regions": 10000, "groups": 8,
+            "histories_per_step": prob.histories, "steps": prob.generations - prob.skip,
+            "histories_per_s": d["histories"] / (d["ms"] / 1000.0),
+            "collisions_per_s": d["collisions"] / (d["ms"] / 1000.0),
+            "ms_per_step": d["ms"] / (prob.generations - prob.skip),
+            "sigma_k_pcm": d["k_sigma"] * 1e5, "k_mean": d["k_mean"],
+            "achieved_GBs": ALG_BYTES_PER_COLLISION * coll_per_launch / (per_launch_ms / 1000.0) / 1e9
+            if per_launch_ms > 0 else 0.0, "launch_shape": d["tuning"]}
+
+
 def cpu_reference_rate(prob, budget_s: float, threads: int):
     """The reference algorithm on the host cores: COMPAT, f32 arithmetic and
     f32 tallies, T threads (histories split as src/mc_code.rs:300-307)."""
@@ -257,6 +308,10 @@ def main():
     ap.add_argument("--reference-budget-s", type=float, default=120.0)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
+    ap.add_argument("--batched-steps", type=int, default=10, help="timed generations of the 256-instance batch (0 = skip)")
+    ap.add_argument("--serve-seconds", type=float, default=20.0, help="Poisson arrival window of the serving run (0 = skip)")
+    ap.add_argument("--serve-rate", type=float, default=200.0)
+    ap.add_argument("--scale-stress", type=int, default=1, help="1 = also run the 10M-history, 200k-cell slab")
     args = ap.parse_args()
     if args.warmup < 3:
         raise SystemExit("--warmup must be >= 3")
@@ -341,6 +396,11 @@ def main():
                "sample": f"1 generation of {n}+{threads} histories of {args.workload}, COMPAT f32, "
                          f"CPU restatement of src/mc_code.rs (reference thread policy)"}
 
+    batched = measure_batched(args.seed, local, args.batched_steps) if args.batched_steps > 0 and arm == "event" else None
+    scale = measure_scale_stress(args.seed, local) if args.scale_stress and arm == "event" else None
+    serving = (measure_serving(args.seed, local, args.serve_seconds, args.serve_rate)
+               if args.serve_seconds > 0 and arm == "event" else None)
+
     if rank == 0:
         line = {
             "metric": "histories/s", "value": value, "unit": "histories/s", "n_gpus": world,
@@ -357,6 +417,7 @@ def main():
             "collisions_per_s": world * d["collisions"] / (ms / 1000.0),
             "gpu_launches": d["launches"], "launch_shape": d["tuning"],
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "plain": plain, "clocks": clk,
+            "batched": batched, "serving": serving, "scale_stress": scale,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
