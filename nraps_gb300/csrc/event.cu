@@ -180,6 +180,9 @@ struct Stage {
     unsigned long long rng[STAGE];
     uint32_t id[STAGE], pk[STAGE];
     uint4 site[STAGE];
+    /* prefetched input records of the warp's current chunk */
+    uint4 pf_a[CHUNK];
+    unsigned long long pf_rng[CHUNK];
 };
 
 /* flush the first n staged survivors of a warp to the out queue (warp-wide) */
@@ -279,6 +282,7 @@ __global__ void __launch_bounds__(256, 3) ev_pass(EvArgs a, int pass, uint32_t K
     unsigned long long* claim = &a.claim[pass];
     const uint32_t slab = (blockIdx.x * WARPS_MAX + w) % NSLAB;
     uint64_t pool_next = 0, pool_end = 0;   /* warp-uniform claimed range     */
+    uint64_t pf_base = 0;                   /* first index of the prefetch    */
     bool exhausted = false;
     uint32_t staged = 0, staged_sites = 0;  /* warp-uniform                   */
     bool slab_full = false;
@@ -290,55 +294,80 @@ __global__ void __launch_bounds__(256, 3) ev_pass(EvArgs a, int pass, uint32_t K
     const EvInst* Ip = &a.inst[0];
     TView tv = t;
     float inv_k = 0.0f;
-    unsigned long long kq_part = 0;
+    unsigned long long kq_part = 0;          /* batched: lane's k score for kq_inst */
+    uint32_t kq_inst = 0;
     uint32_t draws = 0;
     for (;;) {
-        /* ---- hand input particles to idle lanes ---------------------------- */
+        /* ---- hand input particles to idle lanes ----------------------------
+           A warp claims CHUNK input particles with one atomic and prefetches
+           their records (birth site + instance, or queue entry) into shared
+           memory in one coalesced step; idle lanes then take them in order. */
         unsigned need = __ballot_sync(FULL, !have);
         if (need && !exhausted) {
-            uint32_t n_need = __popc(need);
-            uint64_t avail = pool_end - pool_next;
-            uint64_t nb = 0, ne = 0;
-            if (avail < n_need) {
+            if (pool_next == pool_end) {
                 unsigned long long base = 0;
                 if (lane == 0) base = atomicAdd(claim, (unsigned long long)CHUNK);
                 base = __shfl_sync(FULL, base, 0);
-                if (base < n_in) { nb = base; ne = base + CHUNK < n_in ? base + CHUNK : n_in; }
-                else exhausted = true;
-            }
-            uint32_t rank = __popc(need & lt);
-            uint64_t idx = 0;
-            bool got = false;
-            if (!have) {
-                if (rank < avail) { idx = pool_next + rank; got = true; }
-                else if (rank - avail < ne - nb) { idx = nb + (rank - avail); got = true; }
-            }
-            if ((uint64_t)n_need <= avail) pool_next += n_need;
-            else { pool_next = nb + (n_need - avail); pool_end = ne; if (pool_next > pool_end) pool_next = pool_end; }
-            if (got) {
-                if (SOURCE) {
-                    uint32_t inst = 0;
-                    if (!ONE) {
-                        uint32_t lo = 0, hi = a.n_inst;
-                        while (hi - lo > 1) {
-                            uint32_t mid = (lo + hi) >> 1;
-                            if (a.inst_begin[mid] <= idx) lo = mid; else hi = mid;
+                if (base >= n_in) {
+                    exhausted = true;
+                } else {
+                    pool_next = base;
+                    pool_end = base + CHUNK < n_in ? base + CHUNK : n_in;
+                    __syncwarp();          /* every lane is done with the last chunk */
+                    for (uint32_t k = lane; k < (uint32_t)(pool_end - pool_next); k += 32) {
+                        uint64_t idx = pool_next + k;
+                        if (SOURCE) {
+                            uint32_t inst = 0;
+                            if (!ONE) {
+                                uint32_t lo = 0, hi = a.n_inst;
+                                while (hi - lo > 1) {
+                                    uint32_t mid = (lo + hi) >> 1;
+                                    if (a.inst_begin[mid] <= idx) lo = mid; else hi = mid;
+                                }
+                                inst = lo;
+                            }
+                            const EvInst& I = a.inst[inst];
+                            uint32_t local = (uint32_t)(idx - I.hist_begin);
+                            uint4 rec4 = make_uint4(0u, 0xFFFFFFFFu, inst, local);   /* fresh source */
+                            if (BANK) {
+                                const GenState* st = I.st;
+                                uint64_t nbk = st->n_bank;
+                                if (nbk > 0) {
+                                    const nraps_site* bank = I.bank[st->gen & 1];
+                                    nraps_site sv = bank[((uint64_t)local * nbk) / I.N];
+                                    rec4.x = __float_as_uint(sv.x);
+                                    rec4.y = sv.group;
+                                }
+                            }
+                            sg.pf_a[k] = rec4;
+                        } else {
+                            sg.pf_a[k] = make_uint4(__float_as_uint(a.qx[qin][idx]), __float_as_uint(a.qmu[qin][idx]),
+                                                    a.qid[qin][idx], a.qpk[qin][idx]);
+                            sg.pf_rng[k] = a.qrng[qin][idx];
                         }
-                        inst = lo;
                     }
+                    pf_base = pool_next;
+                    __syncwarp();
+                }
+            }
+            uint64_t avail = pool_end - pool_next;
+            uint32_t rank = __popc(need & lt);
+            bool got = !have && rank < avail;
+            uint32_t slot = (uint32_t)(pool_next - pf_base) + rank;
+            uint32_t n_need = __popc(need);
+            pool_next += (uint64_t)n_need < avail ? n_need : avail;
+            if (got) {
+                uint4 r4 = sg.pf_a[slot];
+                if (SOURCE) {
+                    uint32_t inst = r4.z;
                     const EvInst& I = a.inst[inst];
-                    const GenState* st = I.st;
-                    p.id = (uint32_t)idx;
                     p.inst = inst;
-                    p.local = (uint32_t)(idx - I.hist_begin);
+                    p.local = r4.w;
+                    p.id = (uint32_t)(I.hist_begin + p.local);
                     p.seq = 0;
-                    p.rng = nr_pcg32_seeded(nr_generation_seed(I.seed, st->gen), p.local);
-                    uint64_t nbk = BANK ? st->n_bank : 0;
-                    if (nbk > 0) {
-                        const nraps_site* bank = I.bank[st->gen & 1];
-                        uint64_t j = ((uint64_t)p.local * nbk) / I.N;
-                        nraps_site s = bank[j];
-                        p.x = s.x; p.g = s.group;
+                    p.rng = nr_pcg32_seeded(nr_generation_seed(I.seed, I.st->gen), p.local);
+                    if (r4.y != 0xFFFFFFFFu) {
+                        p.x = __uint_as_float(r4.x); p.g = r4.y;
                         p.mu = __fsub_rn(__fmul_rn(2.0f, u24(nr_pcg32_next(&p.rng))), 1.0f);
                     } else {
                         uint32_t cell = I.fuel[((uint64_t)nr_pcg32_next(&p.rng) * I.nfuel) >> 32];
@@ -347,13 +376,13 @@ __global__ void __launch_bounds__(256, 3) ev_pass(EvArgs a, int pass, uint32_t K
                         p.mu = __fsub_rn(__fmul_rn(2.0f, u24(nr_pcg32_next(&p.rng))), 1.0f);
                         p.g = count_below(I.chicdf + (uint32_t)I.cmat[cell] * I.G, I.G, u24(nr_pcg32_next(&p.rng)));
                     }
-                    if (REC && inst == 0) a.rec[p.local].draws += (nbk > 0) ? 1 : 4;
+                    if (REC && inst == 0) a.rec[p.local].draws += (r4.y != 0xFFFFFFFFu) ? 1 : 4;
                 } else {
-                    p.x = a.qx[qin][idx];
-                    p.mu = a.qmu[qin][idx];
-                    p.rng.state = a.qrng[qin][idx];
-                    p.id = a.qid[qin][idx];
-                    uint32_t pk = a.qpk[qin][idx];
+                    p.x = __uint_as_float(r4.x);
+                    p.mu = __uint_as_float(r4.y);
+                    p.id = r4.z;
+                    uint32_t pk = r4.w;
+                    p.rng.state = sg.pf_rng[slot];
                     p.g = pk & 15u;
                     p.inst = (pk >> 4) & 0xFFFu;
                     p.seq = pk >> 16;
@@ -362,12 +391,20 @@ __global__ void __launch_bounds__(256, 3) ev_pass(EvArgs a, int pass, uint32_t K
                     p.rng.inc = ((uint64_t)p.local << 1) | 1ULL;
                 }
                 Ip = &a.inst[ONE ? 0 : p.inst];
-                if (!ONE) tv = global_view(*Ip);
+                if (!ONE) {
+                    tv = global_view(*Ip);
+                    /* consecutive particles of a lane nearly always share an
+                       instance: flush the k score only when it changes */
+                    if (p.inst != kq_inst) {
+                        if (kq_part) atomicAdd(&a.inst[kq_inst].st->kq, kq_part);
+                        kq_part = 0;
+                        kq_inst = p.inst;
+                    }
+                }
                 inv_k = BANK ? Ip->st->inv_kf : 0.0f;
                 have = true;
                 done = 0;
                 events = 0;
-                kq_part = 0;
             }
         }
         if (!__any_sync(FULL, have)) break;
@@ -481,7 +518,6 @@ __global__ void __launch_bounds__(256, 3) ev_pass(EvArgs a, int pass, uint32_t K
                 push = true;
                 have = false;
             }
-            if (!have && !ONE && kq_part) { atomicAdd(&Ip->st->kq, kq_part); kq_part = 0; }
         }
         /* ---- stage survivors; flush 32 at a time ------------------------------ */
         unsigned pm = __ballot_sync(FULL, push);
@@ -502,6 +538,7 @@ __global__ void __launch_bounds__(256, 3) ev_pass(EvArgs a, int pass, uint32_t K
         }
     }
     __syncwarp();
+    if (!ONE && kq_part) atomicAdd(&a.inst[kq_inst].st->kq, kq_part);
     if (staged) flush_particles(a, sg, staged, pass, qout, lane);
     if (BANK && staged_sites) { if (!flush_sites(a, sg, staged_sites, slab, lane)) slab_full = true; }
     if (slab_full && lane == 0) atomicOr(&a.inst[0].st->error, NR_ERR_CAPACITY);
