@@ -48,6 +48,7 @@ extern "C" {
 #define NRAPS_ERR_PENDING    10  /* request admitted but not finished yet       */
 #define NRAPS_ERR_CAPPED     11  /* a history hit the per-history event cap     */
 #define NRAPS_ERR_REJECTED   12  /* request does not fit the memory budget      */
+#define NRAPS_ERR_UNSUPPORTED 13 /* input selects a solver this library lacks   */
 
 /* ---- solver options ----------------------------------------------------- */
 /* mode: which algorithm the generation loop follows.                        */
@@ -392,6 +393,29 @@ int nraps_physics_generation_noalloc(const nraps_device_problem* p, uint64_t see
                                      uint64_t generation, uint64_t max_events,
                                      double* d_tally, double* d_k, uint32_t* d_error,
                                      void* stream);
+
+/* ---- output files and input-file dispatch (no GPU for the first three) ----
+   Text of a float as Rust's Display writes it (plot_solution's to_string(),
+   src/plot_solution.rs:14-34): shortest round-trip digits, positional, no
+   exponent; "1" for 1.0, "-0", "NaN", "inf", "-inf".  Writes a NUL-terminated
+   string; returns its length, or -1 if cap is too small (64 always fits f32,
+   400 always fits f64). */
+int nraps_format_f32(float v, char* buf, uint64_t cap);
+int nraps_format_f64(double v, char* buf, uint64_t cap);
+/* plot_solution (src/plot_solution.rs:7-58): writes dir/vars.csv (assembly
+   length, cells, generations), dir/interface.csv (G flux rows, G
+   assembly-average rows, the fission-source row) and dir/k_eff.csv (k, k_fund)
+   from r's SolutionResults arrays.  dir NULL or "" = the working directory.
+   plot.py is not started. */
+int nraps_write_solution(const char* dir, const nraps_result* r, uint32_t energygroups,
+                         uint64_t cells, uint64_t generations, double assembly_length);
+/* The dispatch of src/main.rs:332-364: process_input(input_path; NULL =
+   "./TestCaseC.txt"), mesh_gen, Monte Carlo with k = 1.0 on ctx when the
+   file has Solution = 1, then nraps_write_solution into out_dir with the
+   last cell's right edge as the assembly length.  Other Solution values
+   select the deterministic solvers: NRAPS_ERR_UNSUPPORTED.  stats_out may be
+   NULL. */
+int nraps_run_input(nraps_ctx* ctx, const char* input_path, const char* out_dir, nraps_stats* stats_out);
 
 /* Text of a status code. */
 const char* nraps_status_string(int status);

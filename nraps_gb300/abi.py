@@ -27,6 +27,7 @@ ERR_NOT_FOUND = 9
 ERR_PENDING = 10
 ERR_CAPPED = 11
 ERR_REJECTED = 12
+ERR_UNSUPPORTED = 13
 
 MODE_COMPAT, MODE_PHYSICS, MODE_BANK = 0, 1, 2
 PREC_FP64, PREC_FP32 = 0, 1

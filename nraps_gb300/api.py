@@ -103,6 +103,11 @@ def load(build_if_missing: bool = True):
     L.nraps_server_clock.argtypes = [vp]
     L.nraps_server_clock.restype = C.c_double
     L.nraps_server_destroy.argtypes = [vp]
+    L.nraps_format_f32.argtypes = [C.c_float, C.c_char_p, C.c_uint64]
+    L.nraps_format_f64.argtypes = [C.c_double, C.c_char_p, C.c_uint64]
+    L.nraps_write_solution.argtypes = [C.c_char_p, P(abi.Result), C.c_uint32, C.c_uint64, C.c_uint64,
+                                       C.c_double]
+    L.nraps_run_input.argtypes = [vp, C.c_char_p, C.c_char_p, P(abi.Stats)]
     L.nraps_status_string.argtypes = [C.c_int]
     L.nraps_status_string.restype = C.c_char_p
     _LIB = L
@@ -216,6 +221,36 @@ def problem_from_input(inp: Input, mesh: MeshArrays, fuel: np.ndarray, k_new: fl
         dx_fuel=inp.delta_x.fuel, dx_water=inp.delta_x.water, k_new=k_new, inv_sigtr=inp.inv_sigtr)
 
 
+# ------------------------------------------------------------ output files --
+def format_f32(v: float) -> str:
+    """Rust `Display` text of an f32 (plot_solution's to_string())."""
+    L = load()
+    buf = C.create_string_buffer(64)
+    n = L.nraps_format_f32(float(np.float32(v)), buf, 64)
+    if n < 0:
+        raise NrapsError(abi.ERR_INVALID, "format buffer too small")
+    return buf.value.decode()
+
+
+def format_f64(v: float) -> str:
+    """Rust `Display` text of an f64."""
+    L = load()
+    buf = C.create_string_buffer(400)
+    n = L.nraps_format_f64(float(v), buf, 400)
+    if n < 0:
+        raise NrapsError(abi.ERR_INVALID, "format buffer too small")
+    return buf.value.decode()
+
+
+def write_solution(res: ResultArrays, generations: int, assembly_length: float, out_dir: str = ".") -> None:
+    """plot_solution (src/plot_solution.rs:7-58): vars.csv, interface.csv and
+    k_eff.csv in out_dir."""
+    L = load()
+    rv = res.view()
+    _check(L.nraps_write_solution(out_dir.encode(), C.byref(rv), res.G, res.cells, generations,
+                                  float(assembly_length)))
+
+
 # ------------------------------------------------------------------ solver --
 class Context:
     """One CUDA context handle (stream + options) of the engine."""
@@ -271,6 +306,13 @@ class Context:
                                          C.byref(pv.delta_x), C.byref(pv.mesh), pv.fuel_indices,
                                          pv.n_fuel, pv.k_new, C.byref(rv)), self.h)
         return res
+
+    def run_input(self, input_path: str = "./TestCaseC.txt", out_dir: str = ".") -> abi.Stats:
+        """The restored main dispatch (src/main.rs:332-364): parse, mesh,
+        Monte Carlo for Solution = 1, write the three CSV files."""
+        st = abi.Stats()
+        _check(self._L.nraps_run_input(self.h, input_path.encode(), out_dir.encode(), C.byref(st)), self.h)
+        return st
 
     def session(self, prob: ProblemArrays) -> "Session":
         return Session(self, prob)

@@ -4,6 +4,8 @@ Each .cu is compiled separately by nvcc for `-gencode arch=compute_103a,
 code=sm_103a`, the host .cpp files by g++, in parallel, then linked into
 nraps_gb300/_build/libnraps_gb300.so against the shared CUDA runtime (the
 same libcudart that PyTorch loads, so streams and events interoperate).
+nraps_main.cpp becomes the command-line program nraps_gb300/_build/nraps,
+which finds the library beside itself.
 
 Flags that carry meaning:
   -ffp-contract=off   host code: table arithmetic must round as written on
@@ -26,6 +28,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libnraps_gb300.so")
+CLI = os.path.join(OUT, "nraps")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = {
@@ -36,7 +39,8 @@ CU_SOURCES = {
     "noalloc.cu": ["--fmad=false"],
     "serve.cu": [],
 }
-CPP_SOURCES = ["host_frontend.cpp", "tables.cpp"]
+CPP_SOURCES = ["host_frontend.cpp", "host_output.cpp", "tables.cpp"]
+CLI_SOURCE = "nraps_main.cpp"  # the `nraps` program, linked against the library
 
 
 def _cuda_home() -> str:
@@ -74,7 +78,7 @@ def _run(cmd: list[str]) -> None:
 def build(force: bool = False, verbose_ptxas: bool = False) -> str:
     os.makedirs(OUT, exist_ok=True)
     deps = _deps()
-    if not force and not _stale(LIB, deps):
+    if not force and not _stale(LIB, deps) and not _stale(CLI, deps):
         return LIB
     cuda = _cuda_home()
     nvcc = os.path.join(cuda, "bin", "nvcc")
@@ -89,19 +93,24 @@ def build(force: bool = False, verbose_ptxas: bool = False) -> str:
             cmd += ["-Xptxas", "-v"]
         jobs.append(cmd)
         objs.append(obj)
-    for src in CPP_SOURCES:
+    for src in CPP_SOURCES + [CLI_SOURCE]:
         obj = os.path.join(OUT, src + ".o")
         cmd = ["g++", "-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-Wall",
                "-I", os.path.join(ROOT, "include"), "-I", os.path.join(cuda, "include"),
                "-c", os.path.join(CSRC, src), "-o", obj]
         jobs.append(cmd)
-        objs.append(obj)
+        if src != CLI_SOURCE:
+            objs.append(obj)
     with cf.ThreadPoolExecutor(max_workers=min(8, len(jobs))) as ex:
         list(ex.map(_run, jobs))
     tmp = LIB + ".tmp"
     _run([nvcc, *ARCH, "-shared", "-cudart", "shared", *objs, "-o", tmp,
           "-Xlinker", "-rpath", "-Xlinker", os.path.join(cuda, "lib64")])
     os.replace(tmp, LIB)
+    tmp = CLI + ".tmp"
+    _run(["g++", os.path.join(OUT, CLI_SOURCE + ".o"), "-o", tmp, "-L", OUT, "-lnraps_gb300",
+          "-Wl,-rpath,$ORIGIN"])
+    os.replace(tmp, CLI)
     return LIB
 
 

@@ -32,6 +32,9 @@ namespace nraps_host {
 static thread_local std::string g_err;
 void set_error(const std::string& msg) { g_err = msg; }
 const char* last_error() { return g_err.c_str(); }
+void set_ctx_error(nraps_ctx* ctx, const std::string& msg) {
+    if (ctx) ctx->err = msg; else g_err = msg;
+}
 }  // namespace nraps_host
 
 using nrint::DevMem;

@@ -335,6 +335,7 @@ const char* nraps_status_string(int s) {
         case NRAPS_ERR_PENDING: return "pending";
         case NRAPS_ERR_CAPPED: return "history event cap reached";
         case NRAPS_ERR_REJECTED: return "rejected: exceeds memory budget";
+        case NRAPS_ERR_UNSUPPORTED: return "unsupported: solver not in this library";
         default: return "unknown status";
     }
 }

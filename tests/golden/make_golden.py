@@ -4,6 +4,12 @@ Inputs: the reference's own input fixtures TestCaseA.txt, TestCaseB.txt and
 TestCaseC.txt (Apache-2.0, copied verbatim as test inputs) and its
 SampleInputFile.txt (legacy keys the parser does not recognise).
 
+Output fixtures: the reference's committed vars.csv and k_eff.csv (verbatim)
+and interface.csv cut to its first 40 fields per row, under plot_output/.
+They were written by an older revision with f64 values, so they pin the text
+layout and the f64 float text of plot_solution (src/plot_solution.rs:36-58),
+not numbers of the current solver.
+
 Expected values: computed by the pure-Python restatement below of
   scan_ascii_chunk / get_index / process_input  (src/process_input.rs:6-175)
   mesh_gen                                       (src/main.rs:85-143)
@@ -116,6 +122,14 @@ def main(ref: str):
             mesh=dict(n_cells=len(mats), matid=mats, mesh_left=lefts, mesh_right=rights, delta_x=dxs,
                       fuel_indices=fuel))
     shutil.copyfile(os.path.join(ref, "SampleInputFile.txt"), os.path.join(HERE, "inputs", "SampleInputFile.txt"))
+    po = os.path.join(HERE, "plot_output")
+    os.makedirs(po, exist_ok=True)
+    for name in ("vars.csv", "k_eff.csv"):
+        shutil.copyfile(os.path.join(ref, name), os.path.join(po, name))
+    with open(os.path.join(ref, "interface.csv"), "rb") as fh, \
+            open(os.path.join(po, "interface_head.csv"), "wb") as out_fh:
+        for line in fh:
+            out_fh.write(b",".join(line.rstrip(b"\n").split(b",")[:40]) + b"\n")
     with open(os.path.join(HERE, "frontend_golden.json"), "w") as fh:
         json.dump(out, fh, indent=0)
     print("wrote", os.path.join(HERE, "frontend_golden.json"))
