@@ -67,6 +67,28 @@ def traffic_per_collision():
     return None
 
 
+def replica_seed(base: int, rank: int) -> int:
+    """Each rank of a multi-GPU run is an independent replica with its own seed."""
+    return base + 1000 * rank
+
+
+def max_over_ranks(x: float, device="cpu") -> float:
+    """The slowest rank's time (all-reduce MAX; identity without a process group)."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return x
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(units_per_rank: float, ms_max: float, world: int) -> float:
+    """Whole-job units/s of `world` replicas that each processed units_per_rank
+    in at most ms_max milliseconds."""
+    return world * units_per_rank / (ms_max / 1000.0)
+
+
 class Clocks:
     def __init__(self, index: int):
         self.proc = None
@@ -335,7 +357,7 @@ def main():
         dist.init_process_group("nccl")
     from nraps_gb300 import abi, api
     api.load()
-    seed = args.seed + 1000 * rank  # independent replicas per rank
+    seed = replica_seed(args.seed, rank)
     prob = make_workload(args.workload, args.seed, args.warmup, args.steps)
 
     arm = args.arm
@@ -353,13 +375,10 @@ def main():
     torch.cuda.synchronize()
     d = measure_device(prob, arm, args.steps, args.warmup, seed, local, shape=args.shape)
     clk = clocks.stop()
-    ms = d["ms"]
+    ms = max_over_ranks(d["ms"], f"cuda:{local}")
     if world > 1:
-        t = torch.tensor([ms], device=f"cuda:{local}", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
         torch.distributed.barrier()
-    value = world * d["histories"] / (ms / 1000.0)
+    value = replica_throughput(d["histories"], ms, world)
 
     # the plain FP64 history-per-thread kernel on the same workload, a few
     # generations (its throughput is the 10x target's denominator)
@@ -374,8 +393,10 @@ def main():
     e2e = None
     if not args.no_e2e:
         e = measure_e2e(prob, arm, seed, local)
-        e2e = {"value": world * e["value"], "unit": "histories/s", "h2d_bytes_per_step": e["h2d"],
-               "d2h_bytes_per_step": e["d2h"], "seconds": e["seconds"], "call": "nraps_monte_carlo"}
+        e_sec = max_over_ranks(e["seconds"], f"cuda:{local}")
+        e2e = {"value": replica_throughput(prob.histories * prob.generations, 1000.0 * e_sec, world),
+               "unit": "histories/s", "h2d_bytes_per_step": e["h2d"],
+               "d2h_bytes_per_step": e["d2h"], "seconds": e_sec, "call": "nraps_monte_carlo"}
 
     peak, peak_kind = peaks()
     per_launch_ms = d["transport_ms"] / max(1, d["transport_launches"])
