@@ -68,6 +68,8 @@ extern "C" {
                                   across every tally cell, track-length tallies */
 #define NRAPS_TRACK_WOODCOCK 1 /* event-based delta tracking, SoA particle queues,
                                   collision estimators (PHYSICS/BANK, FP32 only) */
+/* events_per_pass value: a single transport pass, no re-queueing */
+#define NRAPS_ONE_PASS 0xFFFFFFFFu
 
 typedef struct nraps_opts {
     uint32_t abi_version;        /* must be NRAPS_ABI_VERSION                  */
@@ -81,7 +83,9 @@ typedef struct nraps_opts {
     uint64_t max_events;         /* per-history event cap; 0 = 1<<24           */
     uint32_t block_size;         /* 0 = tuned default                          */
     uint32_t events_per_pass;    /* WOODCOCK: real collisions a particle runs
-                                    before it is re-queued; 0 = tuned default */
+                                    before it is re-queued; 0 = tuned default;
+                                    NRAPS_ONE_PASS = no re-queueing: one pass
+                                    runs every particle to its end          */
     uint32_t passes;             /* WOODCOCK: queue passes per generation before
                                     the drain pass; 0 = tuned default         */
     uint32_t use_graphs;         /* 1 = replay each generation as a CUDA graph */

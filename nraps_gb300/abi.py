@@ -29,6 +29,8 @@ ERR_CAPPED = 11
 ERR_REJECTED = 12
 ERR_UNSUPPORTED = 13
 
+ONE_PASS = 0xFFFFFFFF  # events_per_pass: a single transport pass
+
 MODE_COMPAT, MODE_PHYSICS, MODE_BANK = 0, 1, 2
 PREC_FP64, PREC_FP32 = 0, 1
 TRACK_SURFACE, TRACK_WOODCOCK = 0, 1

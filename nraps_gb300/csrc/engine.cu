@@ -370,8 +370,10 @@ int create_session(nraps_ctx* ctx, const nraps_problem* p, bool with_records, nr
         if (est) return set_err(ctx, est, e2);
         /* tune block size, collisions per pass and pass count unless all given */
         if (!with_records && s->o.block_size == 0 && s->o.events_per_pass == 0 && s->o.passes == 0) {
-            const uint32_t cand[][3] = {{256, 4, 3}, {256, 1, 8}, {256, 2, 4}, {256, 8, 2}, {256, 16, 1},
-                                        {256, 4, 1}, {128, 4, 3}, {128, 8, 2}, {128, 2, 4}, {256, 2, 2}};
+            /* likeliest first: short inactive phases try only the head */
+            const uint32_t cand[][3] = {{256, 16, 1}, {256, NRAPS_ONE_PASS, 0}, {256, 4, 1}, {256, 8, 2},
+                                        {128, 16, 1}, {128, NRAPS_ONE_PASS, 0}, {256, 4, 3}, {256, 2, 4},
+                                        {128, 8, 2}, {256, 1, 8}};
             size_t n = sizeof(cand) / sizeof(cand[0]);
             size_t budget = (size_t)std::min<uint64_t>(s->v.skip, n);
             for (size_t i = 0; i < budget; ++i) {

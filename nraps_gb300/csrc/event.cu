@@ -153,6 +153,53 @@ struct Acc {
     uint32_t coll, virt, absorbed, leaked, capped;
 };
 
+/* Per-instance values a lane needs when it takes a particle or scores a
+   collision.  A single-instance launch keeps one copy per block, filled once;
+   a batched launch keeps one per lane, refilled only when the lane's instance
+   changes (consecutive particles of a lane nearly always share one).  This
+   keeps dependent global loads (descriptor -> GenState -> generation) and the
+   generation-seed hash off the per-particle path. */
+struct Hot {
+    double* tally;
+    unsigned long long gseed;       /* PCG seed of the instance's generation   */
+    unsigned long long hist_begin;
+    uint32_t nc;
+    float inv_k;                    /* (float)(1/k) of the previous generation */
+    uint32_t inst;
+    uint32_t pad;
+};
+
+__device__ __forceinline__ void load_hot(Hot& h, const EvInst& I, uint32_t inst, bool bank) {
+    const GenState* st = I.st;
+    h.tally = I.tally;
+    h.nc = I.nc;
+    h.hist_begin = I.hist_begin;
+    h.gseed = nr_generation_seed(I.seed, st->gen);
+    h.inv_k = bank ? st->inv_kf : 0.0f;
+    h.inst = inst;
+}
+
+/* Bank source of a single-instance launch: the ordered bank of the previous
+   generation, its size B and the histories N; particle i starts at site
+   floor(i*B/N). */
+struct SrcBank {
+    const nraps_site* bank;
+    unsigned long long nbk, N;
+    double inv_N;
+};
+
+/* floor(i*B/N) for i < N < 2^32 and B < 2^32 without a 64-bit division: an
+   FP64 estimate (error below 2^-19 in the quotient) is off by at most one and
+   one integer remainder test corrects it. */
+__device__ __forceinline__ uint64_t bank_site(uint64_t i, const SrcBank& sb) {
+    uint64_t P = i * sb.nbk;
+    uint64_t q = (uint64_t)__dmul_rn(__ull2double_rn(P), sb.inv_N);
+    long long r = (long long)(P - q * sb.N);
+    if (r < 0) --q;
+    else if ((unsigned long long)r >= sb.N) ++q;
+    return q;
+}
+
 __device__ __forceinline__ TView global_view(const EvInst& I) {
     TView t;
     t.xs = I.xs; t.inv_st64 = I.inv_st64; t.kq = I.kq; t.scdf = I.scdf; t.chi = I.chicdf; t.maj = I.maj;
@@ -238,9 +285,22 @@ template <bool SOURCE, bool ONE, bool EXACT, bool BANK, bool REC>
 __global__ void __launch_bounds__(256, 3) ev_pass(EvArgs a, int pass, uint32_t K) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ Stage s_stage[WARPS_MAX];
+    __shared__ Hot s_hot[ONE ? 1 : WARPS_MAX * 32];
+    __shared__ SrcBank s_src;
     TView t;
+    if (!ONE) s_hot[threadIdx.x].inst = 0xFFFFFFFFu;
     if (ONE) {
         const EvInst& I = a.inst[0];
+        if (threadIdx.x == 0) {
+            load_hot(s_hot[0], I, 0, BANK);
+            if (SOURCE && BANK) {
+                const GenState* st = I.st;
+                s_src.bank = I.bank[st->gen & 1];
+                s_src.nbk = st->n_bank;
+                s_src.N = I.N;
+                s_src.inv_N = __drcp_rn((double)I.N);
+            }
+        }
         const uint32_t M = I.M, G = I.G, R = I.R, NB = I.nbins;
         double* s_inv64 = reinterpret_cast<double*>(smem);
         unsigned long long* s_kq = reinterpret_cast<unsigned long long*>(s_inv64 + M * G);
@@ -293,6 +353,7 @@ __global__ void __launch_bounds__(256, 3) ev_pass(EvArgs a, int pass, uint32_t K
     uint64_t events = 0;
     const EvInst* Ip = &a.inst[0];
     TView tv = t;
+    uint32_t tv_inst = 0xFFFFFFFFu;          /* batched: instance tv describes  */
     float inv_k = 0.0f;
     unsigned long long kq_part = 0;          /* batched: lane's k score for kq_inst */
     uint32_t kq_inst = 0;
@@ -329,7 +390,13 @@ __global__ void __launch_bounds__(256, 3) ev_pass(EvArgs a, int pass, uint32_t K
                             const EvInst& I = a.inst[inst];
                             uint32_t local = (uint32_t)(idx - I.hist_begin);
                             uint4 rec4 = make_uint4(0u, 0xFFFFFFFFu, inst, local);   /* fresh source */
-                            if (BANK) {
+                            if (BANK && ONE) {
+                                if (s_src.nbk > 0) {
+                                    nraps_site sv = s_src.bank[bank_site(local, s_src)];
+                                    rec4.x = __float_as_uint(sv.x);
+                                    rec4.y = sv.group;
+                                }
+                            } else if (BANK) {
                                 const GenState* st = I.st;
                                 uint64_t nbk = st->n_bank;
                                 if (nbk > 0) {
@@ -360,16 +427,18 @@ __global__ void __launch_bounds__(256, 3) ev_pass(EvArgs a, int pass, uint32_t K
                 uint4 r4 = sg.pf_a[slot];
                 if (SOURCE) {
                     uint32_t inst = r4.z;
-                    const EvInst& I = a.inst[inst];
+                    Hot& h = s_hot[ONE ? 0 : threadIdx.x];
+                    if (!ONE && h.inst != inst) load_hot(h, a.inst[inst], inst, BANK);
                     p.inst = inst;
                     p.local = r4.w;
-                    p.id = (uint32_t)(I.hist_begin + p.local);
+                    p.id = (uint32_t)(h.hist_begin + p.local);
                     p.seq = 0;
-                    p.rng = nr_pcg32_seeded(nr_generation_seed(I.seed, I.st->gen), p.local);
+                    p.rng = nr_pcg32_seeded(h.gseed, p.local);
                     if (r4.y != 0xFFFFFFFFu) {
                         p.x = __uint_as_float(r4.x); p.g = r4.y;
                         p.mu = __fsub_rn(__fmul_rn(2.0f, u24(nr_pcg32_next(&p.rng))), 1.0f);
                     } else {
+                        const EvInst& I = a.inst[inst];
                         uint32_t cell = I.fuel[((uint64_t)nr_pcg32_next(&p.rng) * I.nfuel) >> 32];
                         float sub = u24(nr_pcg32_next(&p.rng));
                         p.x = __fadd_rn(I.cleft[cell], __fmul_rn(sub, I.cdx[cell]));
@@ -384,15 +453,17 @@ __global__ void __launch_bounds__(256, 3) ev_pass(EvArgs a, int pass, uint32_t K
                     uint32_t pk = r4.w;
                     p.rng.state = sg.pf_rng[slot];
                     p.g = pk & 15u;
-                    p.inst = (pk >> 4) & 0xFFFu;
+                    p.inst = ONE ? 0u : (pk >> 4) & 0xFFFu;
                     p.seq = pk >> 16;
-                    const EvInst& I = a.inst[ONE ? 0 : p.inst];
-                    p.local = (uint32_t)(p.id - I.hist_begin);
+                    Hot& h = s_hot[ONE ? 0 : threadIdx.x];
+                    if (!ONE && h.inst != p.inst) load_hot(h, a.inst[p.inst], p.inst, BANK);
+                    p.local = (uint32_t)(p.id - h.hist_begin);
                     p.rng.inc = ((uint64_t)p.local << 1) | 1ULL;
                 }
                 Ip = &a.inst[ONE ? 0 : p.inst];
-                if (!ONE) {
+                if (!ONE && p.inst != tv_inst) {
                     tv = global_view(*Ip);
+                    tv_inst = p.inst;
                     /* consecutive particles of a lane nearly always share an
                        instance: flush the k score only when it changes */
                     if (p.inst != kq_inst) {
@@ -401,7 +472,7 @@ __global__ void __launch_bounds__(256, 3) ev_pass(EvArgs a, int pass, uint32_t K
                         kq_inst = p.inst;
                     }
                 }
-                inv_k = BANK ? Ip->st->inv_kf : 0.0f;
+                inv_k = s_hot[ONE ? 0 : threadIdx.x].inv_k;
                 have = true;
                 done = 0;
                 events = 0;
@@ -446,7 +517,10 @@ __global__ void __launch_bounds__(256, 3) ev_pass(EvArgs a, int pass, uint32_t K
                         if (k >= nr) k = nr - 1;
                         cell = tv.first[r] + k;
                         const uint32_t j = m * G + p.g;
-                        atomicAdd(&Ip->tally[(uint64_t)p.g * Ip->nc + cell], tv.inv_st64[j]);
+                        {
+                            const Hot& h = s_hot[ONE ? 0 : threadIdx.x];
+                            atomicAdd(&h.tally[(uint64_t)p.g * h.nc + cell], tv.inv_st64[j]);
+                        }
                         unsigned long long q = tv.kq[j];
                         acc.kq += q;
                         kq_part += q;
@@ -796,8 +870,9 @@ int EventEngine::configure(const nraps_opts& o, std::string& err) {
     if (o.block_size) params.block = o.block_size;
     if (o.events_per_pass) params.K = o.events_per_pass;
     if (o.passes) params.passes = o.passes;
+    if (params.K == NRAPS_ONE_PASS) params.passes = 0;     /* every particle to its end in one pass */
     if (params.block != 128 && params.block != 256) { err = "block_size must be 128 or 256 for WOODCOCK"; return NRAPS_ERR_INVALID; }
-    if (params.passes < 1 || params.passes > MAX_PASSES) { err = "passes must be in [1, 16]"; return NRAPS_ERR_INVALID; }
+    if ((params.passes < 1 && params.K != NRAPS_ONE_PASS) || params.passes > MAX_PASSES) { err = "passes must be in [1, 16]"; return NRAPS_ERR_INVALID; }
     if (params.K < 1) { err = "events_per_pass must be >= 1"; return NRAPS_ERR_INVALID; }
     impl_->committed = false;
     return NRAPS_OK;

@@ -42,7 +42,8 @@ struct EvBuffers {
 struct EvParams {
     uint32_t block = 256;   /* threads per block of the transport passes       */
     uint32_t K = 4;         /* real collisions per particle per queue pass     */
-    uint32_t passes = 3;    /* queue passes before the drain pass (>= 1)       */
+    uint32_t passes = 3;    /* queue passes before the drain pass; 0 = one
+                               pass that runs every particle to its end      */
 };
 
 class EventEngine {
