@@ -74,6 +74,38 @@ __global__ void __launch_bounds__(SCAN_THREADS) scan_apply(const uint32_t* count
     }
 }
 
+/* scan_top folded into scan_apply: each tile sums the tile totals before it
+   itself (a block reduction over at most SCAN_CARRY_MAX_TILES values), so a
+   scan of up to 16.7M counts takes two launches instead of three; the last
+   tile writes the grand total. */
+constexpr uint64_t SCAN_CARRY_MAX_TILES = 4096;
+
+__global__ void __launch_bounds__(SCAN_THREADS) scan_apply_carry(const uint32_t* count, uint64_t n,
+                                                                 const uint32_t* tile_sums, uint64_t nb,
+                                                                 uint32_t* offsets, unsigned long long* total) {
+    __shared__ uint32_t sw[33];
+    uint32_t c = 0;
+    for (uint64_t i = threadIdx.x; i < blockIdx.x; i += SCAN_THREADS) c += tile_sums[i];
+    uint32_t ex0;
+    const uint32_t carry = block_excl_scan(c, &ex0, sw);
+    __syncthreads();
+    uint64_t base = (uint64_t)blockIdx.x * SCAN_TILE + (uint64_t)threadIdx.x * SCAN_ITEMS;
+    uint32_t v[SCAN_ITEMS];
+    uint32_t s = 0;
+    for (int i = 0; i < SCAN_ITEMS; ++i) { v[i] = (base + i < n) ? count[base + i] : 0u; s += v[i]; }
+    uint32_t ex;
+    const uint32_t tot = block_excl_scan(s, &ex, sw);
+    uint32_t run = carry + ex;
+    for (int i = 0; i < SCAN_ITEMS; ++i) {
+        if (base + i < n) offsets[base + i] = run;
+        run += v[i];
+    }
+    if (blockIdx.x == nb - 1 && threadIdx.x == 0) {
+        offsets[n] = carry + tot;
+        if (total) *total = carry + tot;
+    }
+}
+
 __global__ void bank_scatter(BankArgs a) {
     const GenState* st = a.st;
     uint64_t n = st->n_sites;
@@ -201,19 +233,23 @@ int launch_exclusive_scan(const uint32_t* count, uint64_t n, uint32_t* block_sum
     uint64_t nb = (n + SCAN_TILE - 1) / SCAN_TILE;
     if (nb == 0) return 0;
     scan_tile_sums<<<(unsigned)nb, SCAN_THREADS, 0, s>>>(count, n, block_sums);
+    if (nb <= SCAN_CARRY_MAX_TILES) {
+        scan_apply_carry<<<(unsigned)nb, SCAN_THREADS, 0, s>>>(count, n, block_sums, nb, offsets, total);
+        return cudaPeekAtLastError() == cudaSuccess ? 2 : -1;
+    }
     scan_top<<<1, SCAN_THREADS, 0, s>>>(block_sums, nb, total, offsets + n);
     scan_apply<<<(unsigned)nb, SCAN_THREADS, 0, s>>>(count, n, block_sums, offsets);
     return cudaPeekAtLastError() == cudaSuccess ? 3 : -1;
 }
 
 int launch_bank_order(const BankArgs& a, cudaStream_t s) {
-    if (launch_exclusive_scan(a.sink.count, a.n_hist, a.block_sums, a.offsets, &a.st->n_bank_next, s) < 0)
-        return -1;
+    int q = launch_exclusive_scan(a.sink.count, a.n_hist, a.block_sums, a.offsets, &a.st->n_bank_next, s);
+    if (q < 0) return -1;
     uint64_t grid = (a.sink.cap + 255) / 256;
     if (grid > 152 * 16) grid = 152 * 16;
     if (grid == 0) grid = 1;
     bank_scatter<<<(unsigned)grid, 256, 0, s>>>(a);
-    return cudaPeekAtLastError() == cudaSuccess ? 4 : -1;
+    return cudaPeekAtLastError() == cudaSuccess ? q + 1 : -1;
 }
 
 int launch_finalize(const FinalizeArgs& a, cudaStream_t s) {

@@ -35,6 +35,10 @@ constexpr uint32_t MAX_PASSES = 16;
 /* one entropy counter per 128-byte line: the fuel cells' site counts then
    spread over every L2 slice instead of a few dozen lines */
 constexpr uint32_t HIST_STRIDE = EV_HIST_STRIDE;
+/* cells of a shared-memory site histogram in the single-instance scatter */
+constexpr uint32_t HIST_SMEM_MAX_CELLS = 12288;
+constexpr int SCATTER_ONE_THREADS = 512;
+constexpr uint32_t SCATTER_ONE_SPLIT = 2;   /* blocks per slab */
 
 struct EvInst {
     const float* xs;          /* [(m*G+g)*4]: sigtr, pabs, nsf_st, inv_st      */
@@ -91,6 +95,9 @@ struct EvArgs {
     uint64_t max_events;
     nraps_history_record* rec;
     int bank;
+    /* single-instance launch with at most HIST_SMEM_MAX_CELLS cells: the
+       scatter counts sites per cell in shared memory */
+    int hist_smem;
 };
 
 /* table view: shared memory (single instance) or the instance's globals */
@@ -340,7 +347,7 @@ __global__ void __launch_bounds__(256, 3) ev_pass(EvArgs a, int pass, uint32_t K
     const int qin = (pass - 1) & 1, qout = pass & 1;
     const uint64_t n_in = SOURCE ? a.n_total : a.qcount[pass - 1];
     unsigned long long* claim = &a.claim[pass];
-    const uint32_t slab = (blockIdx.x * WARPS_MAX + w) % NSLAB;
+    const uint32_t slab = (blockIdx.x * (blockDim.x >> 5) + w) % NSLAB;   /* every slab in use */
     uint64_t pool_next = 0, pool_end = 0;   /* warp-uniform claimed range     */
     uint64_t pf_base = 0;                   /* first index of the prefetch    */
     bool exhausted = false;
@@ -392,18 +399,19 @@ __global__ void __launch_bounds__(256, 3) ev_pass(EvArgs a, int pass, uint32_t K
                             uint4 rec4 = make_uint4(0u, 0xFFFFFFFFu, inst, local);   /* fresh source */
                             if (BANK && ONE) {
                                 if (s_src.nbk > 0) {
-                                    nraps_site sv = s_src.bank[bank_site(local, s_src)];
-                                    rec4.x = __float_as_uint(sv.x);
-                                    rec4.y = sv.group;
+                                    /* one 16-byte load of the site (x, cell, group, pad) */
+                                    uint4 sv = reinterpret_cast<const uint4*>(s_src.bank)[bank_site(local, s_src)];
+                                    rec4.x = sv.x;
+                                    rec4.y = sv.z;
                                 }
                             } else if (BANK) {
                                 const GenState* st = I.st;
                                 uint64_t nbk = st->n_bank;
                                 if (nbk > 0) {
                                     const nraps_site* bank = I.bank[st->gen & 1];
-                                    nraps_site sv = bank[((uint64_t)local * nbk) / I.N];
-                                    rec4.x = __float_as_uint(sv.x);
-                                    rec4.y = sv.group;
+                                    uint4 sv = reinterpret_cast<const uint4*>(bank)[((uint64_t)local * nbk) / I.N];
+                                    rec4.x = sv.x;
+                                    rec4.y = sv.z;
                                 }
                             }
                             sg.pf_a[k] = rec4;
@@ -667,26 +675,78 @@ __global__ void __launch_bounds__(256) ev_scatter(EvArgs a) {
         /* a slab that overflowed keeps stale records: never follow them */
         if (v.z >= a.n_total || inst >= a.n_inst) continue;
         uint32_t cell = v.y & 0x07FFFFFFu;
-        nraps_site s;
-        s.x = __uint_as_float(v.x);
-        s.cell = cell;
-        s.group = v.y >> 27;
-        s.pad = 0;
+        const uint4 s = make_uint4(v.x, cell, v.y >> 27, 0u);   /* nraps_site, one 16-byte store */
         if (ONE) {
             uint64_t pos = (uint64_t)a.offsets[v.z] + (v.w & 0xFFFFu);
             if (pos < cap0) {
-                out0[pos] = s;
+                reinterpret_cast<uint4*>(out0)[pos] = s;
                 atomicAdd(&hist0[(uint64_t)cell * HIST_STRIDE], 1u);
             }
         } else {
             const EvInst& I = a.inst[inst];
             uint64_t pos = (uint64_t)a.offsets[v.z] + (v.w & 0xFFFFu) - a.offsets[I.hist_begin];
             if (pos < I.bank_cap) {
-                I.bank[(I.st->gen + 1) & 1][pos] = s;
+                reinterpret_cast<uint4*>(I.bank[(I.st->gen + 1) & 1])[pos] = s;
                 atomicAdd(&I.hist[(uint64_t)cell * HIST_STRIDE], 1u);
             }
         }
     }
+}
+
+/* Single instance, few cells: one block per slab.  Sites are counted per
+   cell in shared memory and the block adds its non-zero bins to the
+   instance's counters -- a hot fuel cell then costs shared-memory atomics
+   instead of thousands of same-address L2 atomics.  Four sites per thread are
+   loaded before any is used, so each thread keeps four load chains
+   (site -> parent offset) in flight. */
+__global__ void __launch_bounds__(SCATTER_ONE_THREADS) ev_scatter_hist(EvArgs a) {
+    extern __shared__ uint32_t s_h[];
+    const EvInst& I = a.inst[0];
+    const uint32_t nc = I.nc;
+    for (uint32_t c = threadIdx.x; c < nc; c += blockDim.x) s_h[c] = 0;
+    const uint32_t slab = blockIdx.x / SCATTER_ONE_SPLIT, part = blockIdx.x % SCATTER_ONE_SPLIT;
+    uint64_t filled = a.slab_count[slab];
+    if (filled > a.slab_cap) filled = a.slab_cap;
+    /* this block's contiguous share of the slab */
+    const uint64_t per = (filled + SCATTER_ONE_SPLIT - 1) / SCATTER_ONE_SPLIT;
+    const uint64_t lo = per * part;
+    const uint64_t hi = lo + per < filled ? lo + per : filled;
+    const uint4* src = a.sites + (uint64_t)slab * a.slab_cap;
+    nraps_site* out = I.bank[(I.st->gen + 1) & 1];
+    const uint64_t cap = I.bank_cap;
+    __syncthreads();
+    constexpr int U = 4;
+    for (uint64_t j0 = lo + threadIdx.x; j0 < hi; j0 += (uint64_t)U * blockDim.x) {
+        uint4 v[U];
+        uint32_t off[U];
+        bool ok[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            uint64_t j = j0 + (uint64_t)u * blockDim.x;
+            ok[u] = j < hi;
+            v[u] = ok[u] ? src[j] : make_uint4(0, 0, 0, 0);
+            /* a slab that overflowed keeps stale records: never follow them */
+            ok[u] = ok[u] && v[u].z < a.n_total && (v[u].w >> 16) == 0u;
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) off[u] = ok[u] ? a.offsets[v[u].z] : 0u;
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            uint64_t pos = (uint64_t)off[u] + (v[u].w & 0xFFFFu);
+            if (ok[u] && pos < cap) {
+                uint32_t cell = v[u].y & 0x07FFFFFFu;
+                /* one 16-byte store (nraps_site is 4-byte aligned as a type;
+                   the bank itself is 256-byte aligned) */
+                reinterpret_cast<uint4*>(out)[pos] = make_uint4(v[u].x, cell, v[u].y >> 27, 0u);
+                if (cell < nc) atomicAdd(&s_h[cell], 1u);
+            }
+        }
+    }
+    __syncthreads();
+    /* non-zero bins into the instance's strided counters: ~NSLAB additions
+       per fuel cell instead of one per site */
+    for (uint32_t c = threadIdx.x; c < nc; c += blockDim.x)
+        if (s_h[c]) atomicAdd(&I.hist[(uint64_t)c * HIST_STRIDE], s_h[c]);
 }
 
 /* per-instance end of generation: k, entropy, bank size, counters */
@@ -741,34 +801,62 @@ __global__ void __launch_bounds__(FIN_THREADS) ev_finalize(EvArgs a) {
             inst = a.n_inst == 1 ? 0u : find_inst(a.cell_begin, a.n_inst, gc);
             const EvInst& I = a.inst[inst];
             const GenState* st = I.st;
-            uint64_t c = gc - I.cell_begin;
+            const uint64_t c = gc - I.cell_begin;
+            const uint32_t G = I.G, nc = I.nc;
+            double* __restrict__ tally = I.tally;
+            double* __restrict__ flux_acc = I.flux_acc;
+            double* __restrict__ flux_sum = I.flux_sum;
+            double* __restrict__ flux_sq = I.flux_sq;
+            /* every load that does not depend on another is issued up front:
+               the kernel is a handful of L2 round trips, not compute */
             const uint64_t gen = st->gen;
+            const double k = st->k;
+            const double inv_dx = I.inv_dx64[c];
+            const uint32_t m = I.cmat[c];
+            uint32_t cnt = 0;
+            uint64_t B = 0;
+            if (a.bank) {
+                cnt = I.hist[c * HIST_STRIDE];
+                B = a.offsets[I.hist_begin + I.N] - a.offsets[I.hist_begin];
+            }
             if (gen < I.generations) {
                 const bool active = gen >= I.skip;
                 const double fund = 1.0 / (double)(I.generations - I.skip);
-                const double k = st->k;
-                const double phi_scale = I.inv_dx64[c] / (double)I.N;   /* 1/(N dx)   */
+                const double phi_scale = inv_dx / (double)I.N;         /* 1/(N dx)   */
                 const double flux_scale = phi_scale / k;                /* 1/(k N dx) */
                 const double acc_scale = flux_scale * (I.conv_const * k) * fund;
-                uint32_t m = I.cmat[c];
                 double fs = 0.0;
-                for (uint32_t g = 0; g < I.G; ++g) {
-                    uint64_t bin = (uint64_t)g * I.nc + c;
-                    double tl = I.tally[bin];
-                    I.tally[bin] = 0.0;
-                    fs += I.nsf64[m + (uint64_t)I.M * g] * (tl * flux_scale);
-                    if (active) {
-                        double phi = tl * phi_scale;
-                        I.flux_acc[bin] += tl * acc_scale;
-                        I.flux_sum[bin] += phi;
-                        I.flux_sq[bin] += phi * phi;
+                for (uint32_t g0 = 0; g0 < G; g0 += 4) {
+                    double tl[4], nsf[4], fa[4], f1[4], f2[4];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        const uint32_t g = g0 + u;
+                        const uint64_t bin = (uint64_t)g * nc + c;
+                        const bool ok = g < G;
+                        tl[u] = ok ? tally[bin] : 0.0;
+                        nsf[u] = ok ? I.nsf64[m + (uint64_t)I.M * g] : 0.0;
+                        fa[u] = (ok && active) ? flux_acc[bin] : 0.0;
+                        f1[u] = (ok && active) ? flux_sum[bin] : 0.0;
+                        f2[u] = (ok && active) ? flux_sq[bin] : 0.0;
+                    }
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        const uint32_t g = g0 + u;
+                        if (g >= G) break;
+                        const uint64_t bin = (uint64_t)g * nc + c;
+                        tally[bin] = 0.0;
+                        fs += nsf[u] * (tl[u] * flux_scale);
+                        if (active) {
+                            const double phi = tl[u] * phi_scale;
+                            flux_acc[bin] = fa[u] + tl[u] * acc_scale;
+                            flux_sum[bin] = f1[u] + phi;
+                            flux_sq[bin] = f2[u] + phi * phi;
+                        }
                     }
                 }
                 if (active) I.fs_acc[c] += fs * fund;
                 if (a.bank) {
-                    uint32_t cnt = I.hist[c * HIST_STRIDE];
                     I.hist[c * HIST_STRIDE] = 0;
-                    uint64_t B = a.offsets[I.hist_begin + I.N] - a.offsets[I.hist_begin];
                     if (cnt && B) {
                         double pr = (double)cnt / (double)B;
                         h = -pr * nr_log(pr) * 1.4426950408889634;
@@ -799,10 +887,10 @@ __global__ void __launch_bounds__(FIN_THREADS) ev_finalize(EvArgs a) {
     if (!s_last) return;
     __threadfence();
     for (uint32_t i = threadIdx.x; i < a.n_inst; i += blockDim.x) finish_instance(a, i);
+    for (uint32_t p = threadIdx.x; p < 2 * (MAX_PASSES + 2); p += blockDim.x) a.qcount[p] = 0;
+    for (uint32_t q = threadIdx.x; q < NSLAB; q += blockDim.x) a.slab_count[q] = 0;
     __syncthreads();
     if (threadIdx.x == 0) {
-        for (uint32_t p = 0; p < 2 * (MAX_PASSES + 2); ++p) a.qcount[p] = 0;
-        for (uint32_t q = 0; q < NSLAB; ++q) a.slab_count[q] = 0;
         if (a.n_inst > 1) {
             GenState* s = a.stats;
             s->tot_collisions += s->collisions; s->tot_virtual += s->virtual_collisions;
@@ -1068,6 +1156,7 @@ int EventEngine::commit(cudaStream_t s, std::string& err) {
         size_t sb = smem_bytes_for(I.M, I.G, I.R, I.nbins);
         if (sb <= 120 * 1024) { m.one = true; m.smem_bytes = sb; }
     }
+    a.hist_smem = (m.one && bank && m.inst[0]->d.nc <= HIST_SMEM_MAX_CELLS) ? 1 : 0;
     m.committed = true;
     return size_grid();
 }
@@ -1121,8 +1210,16 @@ int EventEngine::enqueue_generation(cudaStream_t s, bool with_finalize, cudaEven
         int q = launch_exclusive_scan(m.count.p, m.n_total, m.block_sums.p, m.offsets.p, nullptr, s);
         if (q < 0) return -1;
         n += q;
-        if (m.one || rec) ev_scatter<true><<<NSLAB * 8, 256, 0, s>>>(a);
-        else ev_scatter<false><<<NSLAB * 8, 256, 0, s>>>(a);
+        if (a.hist_smem) {
+            size_t hb = (size_t)m.inst[0]->d.nc * 4;
+            if (hb > 48 * 1024)
+                cudaFuncSetAttribute(ev_scatter_hist, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hb);
+            ev_scatter_hist<<<NSLAB * SCATTER_ONE_SPLIT, SCATTER_ONE_THREADS, hb, s>>>(a);
+        } else if (m.one || rec) {
+            ev_scatter<true><<<NSLAB * 8, 256, 0, s>>>(a);
+        } else {
+            ev_scatter<false><<<NSLAB * 8, 256, 0, s>>>(a);
+        }
         ++n;
     }
     if (with_finalize) {
