@@ -226,6 +226,8 @@ __host__ __device__ __forceinline__ size_t smem_bytes_for(uint32_t M, uint32_t G
 }
 
 constexpr int WARPS_MAX = 8;        /* blocks of at most 256 threads          */
+struct Stage;
+__host__ __device__ __forceinline__ size_t stage_bytes(uint32_t block);
 constexpr uint32_t CHUNK = 64;      /* particles a warp claims per atomic     */
 constexpr uint32_t STAGE = 64;      /* records a warp stages before a flush   */
 
@@ -238,6 +240,9 @@ struct Stage {
     uint4 pf_a[CHUNK];
     unsigned long long pf_rng[CHUNK];
 };
+
+static_assert(sizeof(Stage) % 16 == 0, "Stage keeps the tables after it 16-byte aligned");
+__host__ __device__ __forceinline__ size_t stage_bytes(uint32_t block) { return (size_t)(block / 32) * sizeof(Stage); }
 
 /* flush the first n staged survivors of a warp to the out queue (warp-wide) */
 __device__ __forceinline__ void flush_particles(const EvArgs& a, Stage& sg, uint32_t n, int pass, int qout,
@@ -289,15 +294,17 @@ __device__ __forceinline__ void move_down(Stage& sg, uint32_t from, uint32_t n, 
  * stage fission sites and particles that completed K real collisions.
  */
 template <bool SOURCE, bool ONE, bool EXACT, bool BANK, bool REC>
-__global__ void __launch_bounds__(256, 3) ev_pass(EvArgs a, int pass, uint32_t K) {
+__global__ void __launch_bounds__(256, ONE ? 4 : 3) ev_pass(EvArgs a, int pass, uint32_t K) {
+    /* dynamic shared memory: one Stage per warp, then (ONE) the tables */
     extern __shared__ __align__(16) unsigned char smem[];
-    __shared__ Stage s_stage[WARPS_MAX];
+    Stage* s_stage = reinterpret_cast<Stage*>(smem);
     __shared__ Hot s_hot[ONE ? 1 : WARPS_MAX * 32];
     __shared__ SrcBank s_src;
     TView t;
     if (!ONE) s_hot[threadIdx.x].inst = 0xFFFFFFFFu;
     if (ONE) {
         const EvInst& I = a.inst[0];
+        unsigned char* tab = smem + (size_t)(blockDim.x >> 5) * sizeof(Stage);
         if (threadIdx.x == 0) {
             load_hot(s_hot[0], I, 0, BANK);
             if (SOURCE && BANK) {
@@ -309,7 +316,7 @@ __global__ void __launch_bounds__(256, 3) ev_pass(EvArgs a, int pass, uint32_t K
             }
         }
         const uint32_t M = I.M, G = I.G, R = I.R, NB = I.nbins;
-        double* s_inv64 = reinterpret_cast<double*>(smem);
+        double* s_inv64 = reinterpret_cast<double*>(tab);
         unsigned long long* s_kq = reinterpret_cast<unsigned long long*>(s_inv64 + M * G);
         float* f = reinterpret_cast<float*>(s_kq + M * G);
         float* s_xs = f;                 f += M * G * 4;
@@ -1052,7 +1059,7 @@ uint64_t EventEngine::shared_bytes() const {
 namespace {
 template <bool SOURCE, bool ONE, bool EXACT, bool BANK, bool REC>
 void set_smem_attr(size_t smem) {
-    static size_t granted = 16 * 1024;          /* below the default dynamic limit */
+    static size_t granted = 48 * 1024;          /* the default dynamic limit         */
     if (smem > granted) {
         cudaFuncSetAttribute(ev_pass<SOURCE, ONE, EXACT, BANK, REC>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -1065,6 +1072,7 @@ int launch_passes(const EvArgs& a, const EvParams& prm, int grid, size_t smem, u
                   cudaStream_t s) {
     int launched = 0;
     uint32_t block = prm.block;
+    smem += stage_bytes(block);
     unsigned g0 = (unsigned)std::min<uint64_t>((n_total + block - 1) / block, (uint64_t)grid);
     if (g0 == 0) g0 = 1;
     set_smem_attr<true, ONE, EXACT, BANK, REC>(smem);
@@ -1171,10 +1179,10 @@ int EventEngine::size_grid() {
     const void* fn = m.one ? (m.exact ? (const void*)ev_pass<false, true, true, true, false>
                                       : (const void*)ev_pass<false, true, false, true, false>)
                            : (const void*)ev_pass<false, false, false, true, false>;
-    if (m.one && m.smem_bytes > 16 * 1024)
-        cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)m.smem_bytes);
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, (int)params.block,
-                                                      m.one ? m.smem_bytes : 0) != cudaSuccess || per_sm < 1)
+    const size_t dyn = stage_bytes(params.block) + (m.one ? m.smem_bytes : 0);
+    if (dyn > 48 * 1024) cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, (int)params.block, dyn) != cudaSuccess ||
+        per_sm < 1)
         per_sm = 1;
     m.grid_blocks = sms * per_sm;
     return NRAPS_OK;
