@@ -157,13 +157,15 @@ ARMS = {
 
 def measure_device(prob, arm: str, steps: int, warmup: int, seed: int, device: int, shape=None):
     """Device-resident throughput: per-step CUDA events on the engine stream.
-    shape = (block, events_per_pass, passes) fixes the event launch shape
+    shape = (block, events_per_pass, passes[, tail_lanes]) fixes the event launch shape
     (no autotuning); None lets the engine tune it over the warm-up."""
     import torch
     from nraps_gb300 import api
     kw = dict(ARMS[arm])
     if shape:
         kw.update(block_size=shape[0], events_per_pass=shape[1], passes=shape[2])
+        if len(shape) > 3:
+            kw.update(tail_lanes=shape[3])
     ctx = api.Context(seed=seed, device=device, **kw)
     s = ctx.session(prob)
     s.set_profile(True)
@@ -339,7 +341,7 @@ def main():
     ap.add_argument("--serve-seconds", type=float, default=20.0, help="Poisson arrival window of the serving run (0 = skip)")
     ap.add_argument("--serve-rate", type=float, default=200.0)
     ap.add_argument("--shape", type=lambda v: tuple(int(x) for x in v.split(",")), default=None,
-                    help="block,events_per_pass,passes: fixed event launch shape (profiling)")
+                    help="block,events_per_pass,passes[,tail_lanes]: fixed event launch shape (profiling)")
     ap.add_argument("--scale-stress", type=int, default=1, help="1 = also run the 10M-history, 200k-cell slab")
     args = ap.parse_args()
     if args.warmup < 3:

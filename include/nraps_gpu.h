@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define NRAPS_ABI_VERSION 1u
+#define NRAPS_ABI_VERSION 2u
 
 /* ---- status codes ------------------------------------------------------- */
 #define NRAPS_OK              0
@@ -94,7 +94,11 @@ typedef struct nraps_opts {
     uint32_t exact_log;          /* WOODCOCK: 1 = flights use the shared software
                                     logarithm (bit-reproducible on a CPU);
                                     0 = the hardware log2 unit (fast)         */
-    uint32_t reserved[6];
+    uint32_t tail_lanes;         /* WOODCOCK: when a pass's input is used up, a
+                                    warp with fewer live particles re-queues
+                                    them for the next pass (needs passes >= 1);
+                                    0 = off                                   */
+    uint32_t reserved[5];
 } nraps_opts;
 
 /* Fill *o with the defaults (FP64 surface tracking, COMPAT, seed 1). */
@@ -243,7 +247,8 @@ int  nraps_session_timing(nraps_session* s, double* transport_ms, double* total_
    is kept; results do not depend on the shape.  tried_ms receives the
    transport time of each candidate tried (up to tried_cap). */
 int  nraps_session_tuning(nraps_session* s, uint32_t* block, uint32_t* events_per_pass,
-                          uint32_t* passes, uint32_t* n_tried, float* tried_ms, uint32_t tried_cap);
+                          uint32_t* passes, uint32_t* tail_lanes, uint32_t* n_tried, float* tried_ms,
+                          uint32_t tried_cap);
 /* generations completed so far (enqueued work included after sync) */
 uint64_t nraps_session_generation(const nraps_session* s);
 void nraps_session_destroy(nraps_session* s);

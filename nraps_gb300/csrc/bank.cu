@@ -28,6 +28,7 @@ namespace {
 constexpr int SCAN_THREADS = 1024;
 constexpr int SCAN_ITEMS = 4;
 constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
+static_assert(SCAN_TILE == (1 << NR_SCAN_TILE_LOG2), "scan tile size");
 
 __global__ void __launch_bounds__(SCAN_THREADS) scan_tile_sums(const uint32_t* count, uint64_t n,
                                                                uint32_t* block_sums) {
@@ -78,7 +79,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) scan_apply(const uint32_t* count
    itself (a block reduction over at most SCAN_CARRY_MAX_TILES values), so a
    scan of up to 16.7M counts takes two launches instead of three; the last
    tile writes the grand total. */
-constexpr uint64_t SCAN_CARRY_MAX_TILES = 4096;
+constexpr uint64_t SCAN_CARRY_MAX_TILES = NR_SCAN_CARRY_MAX_TILES;
 
 __global__ void __launch_bounds__(SCAN_THREADS) scan_apply_carry(const uint32_t* count, uint64_t n,
                                                                  const uint32_t* tile_sums, uint64_t nb,

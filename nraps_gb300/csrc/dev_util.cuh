@@ -51,5 +51,16 @@ __device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v)
     return v;
 }
 
+/* Fire-and-forget global reductions.  Written as PTX `red.global` so that a
+   pointer the compiler cannot prove global (one read from shared memory, say)
+   still becomes a global reduction rather than a generic atomic that returns
+   the old value. */
+__device__ __forceinline__ void red_add_f64(double* p, double v) {
+    asm volatile("red.global.add.f64 [%0], %1;" ::"l"(__cvta_generic_to_global(p)), "d"(v) : "memory");
+}
+__device__ __forceinline__ void red_add_u32(uint32_t* p, uint32_t v) {
+    asm volatile("red.global.add.u32 [%0], %1;" ::"l"(__cvta_generic_to_global(p)), "r"(v) : "memory");
+}
+
 }  // namespace nrdev
 #endif

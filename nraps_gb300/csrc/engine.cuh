@@ -120,6 +120,10 @@ int launch_bank_order(const BankArgs& a, cudaStream_t s);
 /* offsets[i] = sum(count[0..i)), offsets[n] = total (offsets has n+1 slots) */
 int launch_exclusive_scan(const uint32_t* count, uint64_t n, uint32_t* block_sums, uint32_t* offsets,
                           unsigned long long* total, cudaStream_t s);
+/* the scan works on tiles of 2^NR_SCAN_TILE_LOG2 counts; up to
+   NR_SCAN_CARRY_MAX_TILES tiles it takes two launches, beyond that three */
+constexpr int NR_SCAN_TILE_LOG2 = 12;
+constexpr uint64_t NR_SCAN_CARRY_MAX_TILES = 4096;
 int launch_finalize(const FinalizeArgs& a, cudaStream_t s);
 int launch_pcg_stream(uint64_t seed, const uint64_t* streams, uint64_t n, uint32_t per,
                       uint32_t* out, cudaStream_t s);

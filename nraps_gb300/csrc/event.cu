@@ -37,6 +37,8 @@ constexpr uint32_t MAX_PASSES = 16;
 constexpr uint32_t HIST_STRIDE = EV_HIST_STRIDE;
 /* cells of a shared-memory site histogram in the single-instance scatter */
 constexpr uint32_t HIST_SMEM_MAX_CELLS = 12288;
+constexpr uint32_t NLOG2N_TAB = 65536;
+constexpr double LOG2E = 1.4426950408889634;
 constexpr int SCATTER_ONE_THREADS = 512;
 constexpr uint32_t SCATTER_ONE_SPLIT = 2;   /* blocks per slab */
 
@@ -98,6 +100,9 @@ struct EvArgs {
     /* single-instance launch with at most HIST_SMEM_MAX_CELLS cells: the
        scatter counts sites per cell in shared memory */
     int hist_smem;
+    /* n*log2(n) for n < NLOG2N_TAB (FP64, filled once on the host with the
+       shared logarithm): the entropy is log2(B) - sum_c n_c log2(n_c) / B */
+    const double* nlog2n;
 };
 
 /* table view: shared memory (single instance) or the instance's globals */
@@ -294,7 +299,7 @@ __device__ __forceinline__ void move_down(Stage& sg, uint32_t from, uint32_t n, 
  * stage fission sites and particles that completed K real collisions.
  */
 template <bool SOURCE, bool ONE, bool EXACT, bool BANK, bool REC>
-__global__ void __launch_bounds__(256, ONE ? 4 : 3) ev_pass(EvArgs a, int pass, uint32_t K) {
+__global__ void __launch_bounds__(256, ONE ? 4 : 3) ev_pass(EvArgs a, int pass, uint32_t K, uint32_t tail) {
     /* dynamic shared memory: one Stage per warp, then (ONE) the tables */
     extern __shared__ __align__(16) unsigned char smem[];
     Stage* s_stage = reinterpret_cast<Stage*>(smem);
@@ -494,6 +499,29 @@ __global__ void __launch_bounds__(256, ONE ? 4 : 3) ev_pass(EvArgs a, int pass, 
             }
         }
         if (!__any_sync(FULL, have)) break;
+        /* ---- tail hand-off: input used up and few lanes still live -------
+           every live particle goes to the next pass's queue (at the start of
+           its next flight, so its history is unchanged) and the warp leaves */
+        if (tail && exhausted) {
+            const unsigned live = __ballot_sync(FULL, have);
+            if ((uint32_t)__popc(live) < tail) {
+                if (have) {
+                    uint32_t slot = staged + __popc(live & lt);
+                    sg.x[slot] = p.x; sg.mu[slot] = p.mu; sg.rng[slot] = p.rng.state;
+                    sg.id[slot] = p.id; sg.pk[slot] = p.g | (p.inst << 4) | (p.seq << 16);
+                    have = false;
+                }
+                staged += __popc(live);
+                __syncwarp();
+                if (staged >= 32) {
+                    flush_particles(a, sg, 32, pass, qout, lane);
+                    __syncwarp();
+                    move_down(sg, 32, staged - 32, lane, false);
+                    staged -= 32;
+                }
+                break;
+            }
+        }
 
         /* ---- one flight per live lane --------------------------------------- */
         const uint32_t G = tv.G;
@@ -534,7 +562,7 @@ __global__ void __launch_bounds__(256, ONE ? 4 : 3) ev_pass(EvArgs a, int pass, 
                         const uint32_t j = m * G + p.g;
                         {
                             const Hot& h = s_hot[ONE ? 0 : threadIdx.x];
-                            atomicAdd(&h.tally[(uint64_t)p.g * h.nc + cell], tv.inv_st64[j]);
+                            nrdev::red_add_f64(&h.tally[(uint64_t)p.g * h.nc + cell], tv.inv_st64[j]);
                         }
                         unsigned long long q = tv.kq[j];
                         acc.kq += q;
@@ -687,14 +715,14 @@ __global__ void __launch_bounds__(256) ev_scatter(EvArgs a) {
             uint64_t pos = (uint64_t)a.offsets[v.z] + (v.w & 0xFFFFu);
             if (pos < cap0) {
                 reinterpret_cast<uint4*>(out0)[pos] = s;
-                atomicAdd(&hist0[(uint64_t)cell * HIST_STRIDE], 1u);
+                nrdev::red_add_u32(&hist0[(uint64_t)cell * HIST_STRIDE], 1u);
             }
         } else {
             const EvInst& I = a.inst[inst];
             uint64_t pos = (uint64_t)a.offsets[v.z] + (v.w & 0xFFFFu) - a.offsets[I.hist_begin];
             if (pos < I.bank_cap) {
                 reinterpret_cast<uint4*>(I.bank[(I.st->gen + 1) & 1])[pos] = s;
-                atomicAdd(&I.hist[(uint64_t)cell * HIST_STRIDE], 1u);
+                nrdev::red_add_u32(&I.hist[(uint64_t)cell * HIST_STRIDE], 1u);
             }
         }
     }
@@ -708,10 +736,11 @@ __global__ void __launch_bounds__(256) ev_scatter(EvArgs a) {
    (site -> parent offset) in flight. */
 __global__ void __launch_bounds__(SCATTER_ONE_THREADS) ev_scatter_hist(EvArgs a) {
     extern __shared__ uint32_t s_h[];
+    const uint32_t b = blockIdx.x;
     const EvInst& I = a.inst[0];
     const uint32_t nc = I.nc;
     for (uint32_t c = threadIdx.x; c < nc; c += blockDim.x) s_h[c] = 0;
-    const uint32_t slab = blockIdx.x / SCATTER_ONE_SPLIT, part = blockIdx.x % SCATTER_ONE_SPLIT;
+    const uint32_t slab = b / SCATTER_ONE_SPLIT, part = b % SCATTER_ONE_SPLIT;
     uint64_t filled = a.slab_count[slab];
     if (filled > a.slab_cap) filled = a.slab_cap;
     /* this block's contiguous share of the slab */
@@ -753,32 +782,116 @@ __global__ void __launch_bounds__(SCATTER_ONE_THREADS) ev_scatter_hist(EvArgs a)
     /* non-zero bins into the instance's strided counters: ~NSLAB additions
        per fuel cell instead of one per site */
     for (uint32_t c = threadIdx.x; c < nc; c += blockDim.x)
-        if (s_h[c]) atomicAdd(&I.hist[(uint64_t)c * HIST_STRIDE], s_h[c]);
+        if (s_h[c]) nrdev::red_add_u32(&I.hist[(uint64_t)c * HIST_STRIDE], s_h[c]);
+}
+
+/* block-wide: pass counters and slab fills back to zero for the next
+   generation (called by the block that closes a generation) */
+__device__ __forceinline__ void reset_pass_counters(const EvArgs& a) {
+    for (uint32_t p = threadIdx.x; p < 2 * (MAX_PASSES + 2); p += blockDim.x) a.qcount[p] = 0;
+    for (uint32_t q = threadIdx.x; q < NSLAB; q += blockDim.x) a.slab_count[q] = 0;
+}
+
+/* n log2(n) of a cell's site count (exact table below NLOG2N_TAB) */
+__device__ __forceinline__ double nlog2n(const EvArgs& a, uint32_t n) {
+    return n < NLOG2N_TAB ? a.nlog2n[n] : (double)n * nr_log((double)n) * LOG2E;
+}
+
+/*
+ * One cell of one instance at the end of a generation: reads and clears its
+ * G tally bins and, in active generations, accumulates flux, flux moments
+ * and fission source (multiplications by precomputed reciprocals: FP64
+ * division is slow on this part).  Every load that does not depend on
+ * another is issued before the first store: the work is a few L2 round
+ * trips, not arithmetic.
+ */
+__device__ __forceinline__ void fold_cell(const EvInst& I, uint64_t c, uint64_t gen, double k) {
+    const uint32_t G = I.G, nc = I.nc;
+    double* __restrict__ tally = I.tally;
+    double* __restrict__ flux_acc = I.flux_acc;
+    double* __restrict__ flux_sum = I.flux_sum;
+    double* __restrict__ flux_sq = I.flux_sq;
+    const double inv_dx = I.inv_dx64[c];
+    const uint32_t m = I.cmat[c];
+    const bool active = gen >= I.skip;
+    const double fund = 1.0 / (double)(I.generations - I.skip);
+    const double phi_scale = inv_dx / (double)I.N;         /* 1/(N dx)   */
+    const double flux_scale = phi_scale / k;                /* 1/(k N dx) */
+    const double acc_scale = flux_scale * (I.conv_const * k) * fund;
+    double fs = 0.0;
+    for (uint32_t g0 = 0; g0 < G; g0 += 4) {
+        double tl[4], nsf[4], fa[4], f1[4], f2[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const uint32_t g = g0 + u;
+            const uint64_t bin = (uint64_t)g * nc + c;
+            const bool ok = g < G;
+            tl[u] = ok ? tally[bin] : 0.0;
+            nsf[u] = ok ? I.nsf64[m + (uint64_t)I.M * g] : 0.0;
+            fa[u] = (ok && active) ? flux_acc[bin] : 0.0;
+            f1[u] = (ok && active) ? flux_sum[bin] : 0.0;
+            f2[u] = (ok && active) ? flux_sq[bin] : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const uint32_t g = g0 + u;
+            if (g >= G) break;
+            const uint64_t bin = (uint64_t)g * nc + c;
+            tally[bin] = 0.0;
+            fs += nsf[u] * (tl[u] * flux_scale);
+            if (active) {
+                const double phi = tl[u] * phi_scale;
+                flux_acc[bin] = fa[u] + tl[u] * acc_scale;
+                flux_sum[bin] = f1[u] + phi;
+                flux_sq[bin] = f2[u] + phi * phi;
+            }
+        }
+    }
+    if (active) I.fs_acc[c] += fs * fund;
 }
 
 /* per-instance end of generation: k, entropy, bank size, counters */
-__device__ void finish_instance(const EvArgs& a, uint32_t i) {
+__device__ void finish_instance(const EvArgs& a, uint32_t i, const double* h_given = nullptr) {
     const EvInst& I = a.inst[i];
     GenState* st = I.st;
-    uint64_t gen = st->gen;
+    /* every load first: this runs on one thread at the tail of the launch */
+    const uint64_t gen = st->gen;
+    const unsigned long long kq = st->kq;
+    const double h = h_given ? *h_given : st->h_acc;
+    const double ksum = st->ksum, ksum2 = st->ksum2;
+    const unsigned long long nactive = st->nactive, tot_sites = st->tot_sites, tot_hist = st->tot_histories;
+    const unsigned int err0 = st->error;
+    unsigned long long B = 0;
+    if (a.bank) B = a.offsets[I.hist_begin + I.N] - a.offsets[I.hist_begin];
+    unsigned long long c[5] = {0, 0, 0, 0, 0}, t[5] = {0, 0, 0, 0, 0};
+    if (a.n_inst == 1) {
+        c[0] = st->collisions; c[1] = st->virtual_collisions; c[2] = st->absorbed; c[3] = st->leaked;
+        c[4] = st->capped;
+        t[0] = st->tot_collisions; t[1] = st->tot_virtual; t[2] = st->tot_absorbed; t[3] = st->tot_leaked;
+        t[4] = st->tot_capped;
+    }
     if (gen >= I.generations) return;
-    double k_new = nr_unfix(st->kq) / (double)I.N;
+    const double k_new = nr_unfix(kq) / (double)I.N;
     I.k64[gen] = k_new;
-    if (gen >= I.skip) { st->ksum += k_new; st->ksum2 += k_new * k_new; st->nactive++; }
-    I.entropy[gen] = a.bank ? st->h_acc : 0.0;
+    if (gen >= I.skip) { st->ksum = ksum + k_new; st->ksum2 = ksum2 + k_new * k_new; st->nactive = nactive + 1; }
+    unsigned int err = err0;
     if (a.bank) {
-        unsigned long long B = a.offsets[I.hist_begin + I.N] - a.offsets[I.hist_begin];
-        st->tot_sites += B;
-        if (B > I.bank_cap) { B = I.bank_cap; st->error |= NR_ERR_CAPACITY; }
+        /* h holds -sum_c n_c log2(n_c) / B */
+        I.entropy[gen] = B ? nr_log((double)B) * LOG2E + h : 0.0;
+        st->tot_sites = tot_sites + B;
+        if (B > I.bank_cap) { B = I.bank_cap; err |= NR_ERR_CAPACITY; }
         st->n_bank = B;
-        if (B == 0) st->error |= NR_ERR_EMPTY;
+        if (B == 0) err |= NR_ERR_EMPTY;
+        if (err != err0) st->error = err;
+    } else {
+        I.entropy[gen] = 0.0;
     }
     if (a.n_inst == 1) {
-        st->tot_collisions += st->collisions; st->tot_virtual += st->virtual_collisions;
-        st->tot_absorbed += st->absorbed; st->tot_leaked += st->leaked; st->tot_capped += st->capped;
+        st->tot_collisions = t[0] + c[0]; st->tot_virtual = t[1] + c[1]; st->tot_absorbed = t[2] + c[2];
+        st->tot_leaked = t[3] + c[3]; st->tot_capped = t[4] + c[4];
         st->collisions = st->virtual_collisions = st->absorbed = st->leaked = st->capped = 0;
     }
-    st->tot_histories += I.N;
+    st->tot_histories = tot_hist + I.N;
     st->kq = 0;
     st->h_acc = 0.0;
     st->n_sites = 0;
@@ -809,17 +922,8 @@ __global__ void __launch_bounds__(FIN_THREADS) ev_finalize(EvArgs a) {
             const EvInst& I = a.inst[inst];
             const GenState* st = I.st;
             const uint64_t c = gc - I.cell_begin;
-            const uint32_t G = I.G, nc = I.nc;
-            double* __restrict__ tally = I.tally;
-            double* __restrict__ flux_acc = I.flux_acc;
-            double* __restrict__ flux_sum = I.flux_sum;
-            double* __restrict__ flux_sq = I.flux_sq;
-            /* every load that does not depend on another is issued up front:
-               the kernel is a handful of L2 round trips, not compute */
             const uint64_t gen = st->gen;
             const double k = st->k;
-            const double inv_dx = I.inv_dx64[c];
-            const uint32_t m = I.cmat[c];
             uint32_t cnt = 0;
             uint64_t B = 0;
             if (a.bank) {
@@ -827,47 +931,10 @@ __global__ void __launch_bounds__(FIN_THREADS) ev_finalize(EvArgs a) {
                 B = a.offsets[I.hist_begin + I.N] - a.offsets[I.hist_begin];
             }
             if (gen < I.generations) {
-                const bool active = gen >= I.skip;
-                const double fund = 1.0 / (double)(I.generations - I.skip);
-                const double phi_scale = inv_dx / (double)I.N;         /* 1/(N dx)   */
-                const double flux_scale = phi_scale / k;                /* 1/(k N dx) */
-                const double acc_scale = flux_scale * (I.conv_const * k) * fund;
-                double fs = 0.0;
-                for (uint32_t g0 = 0; g0 < G; g0 += 4) {
-                    double tl[4], nsf[4], fa[4], f1[4], f2[4];
-#pragma unroll
-                    for (int u = 0; u < 4; ++u) {
-                        const uint32_t g = g0 + u;
-                        const uint64_t bin = (uint64_t)g * nc + c;
-                        const bool ok = g < G;
-                        tl[u] = ok ? tally[bin] : 0.0;
-                        nsf[u] = ok ? I.nsf64[m + (uint64_t)I.M * g] : 0.0;
-                        fa[u] = (ok && active) ? flux_acc[bin] : 0.0;
-                        f1[u] = (ok && active) ? flux_sum[bin] : 0.0;
-                        f2[u] = (ok && active) ? flux_sq[bin] : 0.0;
-                    }
-#pragma unroll
-                    for (int u = 0; u < 4; ++u) {
-                        const uint32_t g = g0 + u;
-                        if (g >= G) break;
-                        const uint64_t bin = (uint64_t)g * nc + c;
-                        tally[bin] = 0.0;
-                        fs += nsf[u] * (tl[u] * flux_scale);
-                        if (active) {
-                            const double phi = tl[u] * phi_scale;
-                            flux_acc[bin] = fa[u] + tl[u] * acc_scale;
-                            flux_sum[bin] = f1[u] + phi;
-                            flux_sq[bin] = f2[u] + phi * phi;
-                        }
-                    }
-                }
-                if (active) I.fs_acc[c] += fs * fund;
+                fold_cell(I, c, gen, k);
                 if (a.bank) {
                     I.hist[c * HIST_STRIDE] = 0;
-                    if (cnt && B) {
-                        double pr = (double)cnt / (double)B;
-                        h = -pr * nr_log(pr) * 1.4426950408889634;
-                    }
+                    if (cnt && B) h = -nlog2n(a, cnt) / (double)B;
                 }
             }
         }
@@ -894,8 +961,7 @@ __global__ void __launch_bounds__(FIN_THREADS) ev_finalize(EvArgs a) {
     if (!s_last) return;
     __threadfence();
     for (uint32_t i = threadIdx.x; i < a.n_inst; i += blockDim.x) finish_instance(a, i);
-    for (uint32_t p = threadIdx.x; p < 2 * (MAX_PASSES + 2); p += blockDim.x) a.qcount[p] = 0;
-    for (uint32_t q = threadIdx.x; q < NSLAB; q += blockDim.x) a.slab_count[q] = 0;
+    reset_pass_counters(a);
     __syncthreads();
     if (threadIdx.x == 0) {
         if (a.n_inst > 1) {
@@ -944,6 +1010,7 @@ struct EventEngine::Impl {
     DBuf<uint4> sites;
     DBuf<uint32_t> count, offsets, block_sums;
     DBuf<GenState> bstats;
+    DBuf<double> nlog2n;
     uint64_t n_total = 0, n_cells_total = 0, slab_cap = 0, cap_total = 0, cap_inst = 0;
     nraps_history_record* rec = nullptr;
     EvArgs args{};
@@ -965,7 +1032,10 @@ int EventEngine::configure(const nraps_opts& o, std::string& err) {
     if (o.block_size) params.block = o.block_size;
     if (o.events_per_pass) params.K = o.events_per_pass;
     if (o.passes) params.passes = o.passes;
-    if (params.K == NRAPS_ONE_PASS) params.passes = 0;     /* every particle to its end in one pass */
+    params.tail = o.tail_lanes;
+    if (params.K == NRAPS_ONE_PASS && o.passes == 0) params.passes = 0;  /* every particle to its end in one pass */
+    if (params.tail > 32) { err = "tail_lanes must be at most 32"; return NRAPS_ERR_INVALID; }
+    if (params.tail && params.passes == 0) { err = "tail_lanes needs a following pass (passes >= 1)"; return NRAPS_ERR_INVALID; }
     if (params.block != 128 && params.block != 256) { err = "block_size must be 128 or 256 for WOODCOCK"; return NRAPS_ERR_INVALID; }
     if ((params.passes < 1 && params.K != NRAPS_ONE_PASS) || params.passes > MAX_PASSES) { err = "passes must be in [1, 16]"; return NRAPS_ERR_INVALID; }
     if (params.K < 1) { err = "events_per_pass must be >= 1"; return NRAPS_ERR_INVALID; }
@@ -1078,11 +1148,13 @@ int launch_passes(const EvArgs& a, const EvParams& prm, int grid, size_t smem, u
     set_smem_attr<true, ONE, EXACT, BANK, REC>(smem);
     set_smem_attr<false, ONE, EXACT, BANK, REC>(smem);
     uint32_t P = prm.passes;
-    ev_pass<true, ONE, EXACT, BANK, REC><<<g0, block, smem, s>>>(a, 0, P == 0 ? 0xFFFFFFFFu : prm.K);
+    ev_pass<true, ONE, EXACT, BANK, REC><<<g0, block, smem, s>>>(a, 0, P == 0 ? 0xFFFFFFFFu : prm.K,
+                                                                 P == 0 ? 0u : prm.tail);
     ++launched;
     for (uint32_t p = 1; p <= P; ++p) {
-        uint32_t K = (p == P) ? 0xFFFFFFFFu : prm.K;
-        ev_pass<false, ONE, EXACT, BANK, REC><<<(unsigned)grid, block, smem, s>>>(a, (int)p, K);
+        const bool last = p == P;
+        ev_pass<false, ONE, EXACT, BANK, REC><<<(unsigned)grid, block, smem, s>>>(
+            a, (int)p, last ? 0xFFFFFFFFu : prm.K, last ? 0u : prm.tail);
         ++launched;
     }
     return cudaPeekAtLastError() == cudaSuccess ? launched : -1;
@@ -1165,6 +1237,16 @@ int EventEngine::commit(cudaStream_t s, std::string& err) {
         if (sb <= 120 * 1024) { m.one = true; m.smem_bytes = sb; }
     }
     a.hist_smem = (m.one && bank && m.inst[0]->d.nc <= HIST_SMEM_MAX_CELLS) ? 1 : 0;
+    if (!m.nlog2n.p) {
+        std::vector<double> t(NLOG2N_TAB, 0.0);
+        for (uint32_t i = 2; i < NLOG2N_TAB; ++i) t[i] = (double)i * nr_log((double)i) * LOG2E;
+        if (m.nlog2n.alloc(NLOG2N_TAB) != cudaSuccess ||
+            cudaMemcpy(m.nlog2n.p, t.data(), NLOG2N_TAB * 8, cudaMemcpyHostToDevice) != cudaSuccess) {
+            err = "event engine buffers: entropy table";
+            return NRAPS_ERR_NOMEM;
+        }
+    }
+    a.nlog2n = m.nlog2n.p;
     m.committed = true;
     return size_grid();
 }
@@ -1193,10 +1275,10 @@ uint64_t EventEngine::launches_per_generation() const { return 1 + params.passes
 int EventEngine::enqueue_generation(cudaStream_t s, bool with_finalize, cudaEvent_t t0, cudaEvent_t t1) {
     Impl& m = *impl_;
     if (!m.committed) return -1;
-    if (t0) cudaEventRecord(t0, s);
     const EvArgs& a = m.args;
     bool bank = m.mode == NRAPS_MODE_BANK;
     bool rec = m.rec != nullptr;
+    if (t0) cudaEventRecord(t0, s);
     int r;
 #define EV_LAUNCH(ONE, EXACT, BANK, REC) \
     r = launch_passes<ONE, EXACT, BANK, REC>(a, params, m.grid_blocks, ONE ? m.smem_bytes : 0, m.n_total, s)
@@ -1219,7 +1301,7 @@ int EventEngine::enqueue_generation(cudaStream_t s, bool with_finalize, cudaEven
         if (q < 0) return -1;
         n += q;
         if (a.hist_smem) {
-            size_t hb = (size_t)m.inst[0]->d.nc * 4;
+            const size_t hb = (size_t)m.inst[0]->d.nc * 4;
             if (hb > 48 * 1024)
                 cudaFuncSetAttribute(ev_scatter_hist, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hb);
             ev_scatter_hist<<<NSLAB * SCATTER_ONE_SPLIT, SCATTER_ONE_THREADS, hb, s>>>(a);

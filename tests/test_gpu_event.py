@@ -19,7 +19,8 @@ pytestmark = pytest.mark.gpu
 SHAPES = [dict(events_per_pass=1, passes=4, block_size=128),
           dict(events_per_pass=4, passes=2, block_size=256),
           dict(events_per_pass=16, passes=1, block_size=256),
-          dict(events_per_pass=abi.ONE_PASS, passes=0, block_size=256)]
+          dict(events_per_pass=abi.ONE_PASS, passes=0, block_size=256),
+          dict(events_per_pass=abi.ONE_PASS, passes=1, block_size=128, tail_lanes=12)]
 
 
 def small(hist=3000, gens=12, skip=4, seed=3):
@@ -35,7 +36,7 @@ def _records_equal(g, w):
         assert bad.size == 0, (f, bad[:5], g[f][bad[:5]], w[f][bad[:5]])
 
 
-@pytest.mark.parametrize("shape", SHAPES, ids=["K1P4b128", "K4P2b256", "K16P1b256", "onepass256"])
+@pytest.mark.parametrize("shape", SHAPES, ids=["K1P4b128", "K4P2b256", "K16P1b256", "onepass256", "tail12b128"])
 @pytest.mark.parametrize("mode", [abi.MODE_PHYSICS, abi.MODE_BANK])
 def test_event_trace_bitexact(ctx_factory, mode, shape):
     p = small()
