@@ -37,6 +37,31 @@ constexpr uint32_t MAX_PASSES = 16;
 constexpr uint32_t HIST_STRIDE = EV_HIST_STRIDE;
 /* cells of a shared-memory site histogram in the single-instance scatter */
 constexpr uint32_t HIST_SMEM_MAX_CELLS = 12288;
+/*
+ * Unsigned division by an invariant divisor d (1 <= d < 2^63) as a 64x64
+ * multiply-high, a subtraction and two shifts (Granlund & Montgomery,
+ * "Division by invariant integers using multiplication", PLDI 1994, fig. 4.1):
+ * with l = ceil(log2 d) and m = floor(2^64 (2^l - d) / d) + 1,
+ * q = (t + ((n - t) >> min(l,1))) >> max(l-1,0) where t = mulhi(m, n).
+ */
+struct NDiv {
+    unsigned long long m;
+    uint32_t sh1, sh2;
+    __host__ static NDiv make(uint64_t d) {
+        NDiv r;
+        uint32_t l = 0;
+        while (l < 63 && (1ULL << l) < d) ++l;
+        r.m = (unsigned long long)((((unsigned __int128)((1ULL << l) - d)) << 64) / d) + 1ULL;
+        r.sh1 = l < 1 ? l : 1u;
+        r.sh2 = l > 1 ? l - 1 : 0u;
+        return r;
+    }
+    __device__ __forceinline__ uint64_t div(uint64_t n) const {
+        const uint64_t t = __umul64hi(m, n);
+        return (t + ((n - t) >> sh1)) >> sh2;
+    }
+};
+
 constexpr uint32_t NLOG2N_TAB = 65536;
 constexpr double LOG2E = 1.4426950408889634;
 constexpr int SCATTER_ONE_THREADS = 512;
@@ -64,6 +89,7 @@ struct EvInst {
     uint32_t M, G, R, nc, nbins, nfuel;
     float L, inv_binw, boundl, boundr;
     uint64_t hist_begin, N, seed;
+    NDiv ndiv;                /* division by N                                 */
     GenState* st;
     double* tally;
     double *flux_acc, *fs_acc, *flux_sum, *flux_sq, *k64, *entropy;
@@ -192,24 +218,19 @@ __device__ __forceinline__ void load_hot(Hot& h, const EvInst& I, uint32_t inst,
 }
 
 /* Bank source of a single-instance launch: the ordered bank of the previous
-   generation, its size B and the histories N; particle i starts at site
-   floor(i*B/N). */
+   generation, its size B and the divisor N (histories); particle i starts at
+   site floor(i*B/N). */
 struct SrcBank {
     const nraps_site* bank;
-    unsigned long long nbk, N;
-    double inv_N;
+    unsigned long long nbk;
+    NDiv ndiv;
 };
 
-/* floor(i*B/N) for i < N < 2^32 and B < 2^32 without a 64-bit division: an
-   FP64 estimate (error below 2^-19 in the quotient) is off by at most one and
-   one integer remainder test corrects it. */
-__device__ __forceinline__ uint64_t bank_site(uint64_t i, const SrcBank& sb) {
-    uint64_t P = i * sb.nbk;
-    uint64_t q = (uint64_t)__dmul_rn(__ull2double_rn(P), sb.inv_N);
-    long long r = (long long)(P - q * sb.N);
-    if (r < 0) --q;
-    else if ((unsigned long long)r >= sb.N) ++q;
-    return q;
+/* floor(i*B/N) for i < N <= 2^32 and B < 2^32: the product fits 64 bits and
+   the division by N is a multiply-high with N's invariant reciprocal
+   (integer pipes only; FP64 and 64-bit division are slow on this part) */
+__device__ __forceinline__ uint64_t bank_site(uint64_t i, uint64_t nbk, const NDiv& nd) {
+    return nd.div(i * nbk);
 }
 
 __device__ __forceinline__ TView global_view(const EvInst& I) {
@@ -316,8 +337,7 @@ __global__ void __launch_bounds__(256, ONE ? 4 : 3) ev_pass(EvArgs a, int pass, 
                 const GenState* st = I.st;
                 s_src.bank = I.bank[st->gen & 1];
                 s_src.nbk = st->n_bank;
-                s_src.N = I.N;
-                s_src.inv_N = __drcp_rn((double)I.N);
+                s_src.ndiv = I.ndiv;
             }
         }
         const uint32_t M = I.M, G = I.G, R = I.R, NB = I.nbins;
@@ -412,7 +432,7 @@ __global__ void __launch_bounds__(256, ONE ? 4 : 3) ev_pass(EvArgs a, int pass, 
                             if (BANK && ONE) {
                                 if (s_src.nbk > 0) {
                                     /* one 16-byte load of the site (x, cell, group, pad) */
-                                    uint4 sv = reinterpret_cast<const uint4*>(s_src.bank)[bank_site(local, s_src)];
+                                    uint4 sv = reinterpret_cast<const uint4*>(s_src.bank)[bank_site(local, s_src.nbk, s_src.ndiv)];
                                     rec4.x = sv.x;
                                     rec4.y = sv.z;
                                 }
@@ -421,7 +441,7 @@ __global__ void __launch_bounds__(256, ONE ? 4 : 3) ev_pass(EvArgs a, int pass, 
                                 uint64_t nbk = st->n_bank;
                                 if (nbk > 0) {
                                     const nraps_site* bank = I.bank[st->gen & 1];
-                                    uint4 sv = reinterpret_cast<const uint4*>(bank)[((uint64_t)local * nbk) / I.N];
+                                    uint4 sv = reinterpret_cast<const uint4*>(bank)[bank_site(local, nbk, I.ndiv)];
                                     rec4.x = sv.x;
                                     rec4.y = sv.z;
                                 }
@@ -1090,7 +1110,7 @@ int EventEngine::add_instance(const nraps_problem& p, const EvBuffers& b, std::s
     d.nsf64 = (const double*)(B + o_nsf); d.inv_dx64 = (const double*)(B + o_idx);
     d.M = h.M; d.G = h.G; d.R = h.R; d.nc = h.nc; d.nbins = h.nbins; d.nfuel = h.nfuel;
     d.L = h.L; d.inv_binw = h.inv_binw; d.boundl = h.boundl; d.boundr = h.boundr;
-    d.N = p.variables.histories; d.seed = b.seed;
+    d.N = p.variables.histories; d.seed = b.seed; d.ndiv = NDiv::make(d.N);
     d.st = b.st; d.tally = b.tally;
     d.flux_acc = b.flux_acc; d.fs_acc = b.fs_acc; d.flux_sum = b.flux_sum; d.flux_sq = b.flux_sq;
     d.k64 = b.k64; d.entropy = b.entropy;
