@@ -217,6 +217,13 @@ __device__ __forceinline__ void load_hot(Hot& h, const EvInst& I, uint32_t inst,
     h.inst = inst;
 }
 
+/* Batched launches: per lane, the generation seed and first history of the
+   instance whose birth records the lane last prefetched. */
+struct PfHot {
+    unsigned long long gseed, hist_begin;
+    uint32_t inst, pad;
+};
+
 /* Bank source of a single-instance launch: the ordered bank of the previous
    generation, its size B and the divisor N (histories); particle i starts at
    site floor(i*B/N). */
@@ -325,9 +332,13 @@ __global__ void __launch_bounds__(256, ONE ? 4 : 3) ev_pass(EvArgs a, int pass, 
     extern __shared__ __align__(16) unsigned char smem[];
     Stage* s_stage = reinterpret_cast<Stage*>(smem);
     __shared__ Hot s_hot[ONE ? 1 : WARPS_MAX * 32];
+    __shared__ PfHot s_pf[ONE ? 1 : WARPS_MAX * 32];
     __shared__ SrcBank s_src;
     TView t;
-    if (!ONE) s_hot[threadIdx.x].inst = 0xFFFFFFFFu;
+    if (!ONE) {
+        s_hot[threadIdx.x].inst = 0xFFFFFFFFu;
+        s_pf[threadIdx.x].inst = 0xFFFFFFFFu;
+    }
     if (ONE) {
         const EvInst& I = a.inst[0];
         unsigned char* tab = smem + (size_t)(blockDim.x >> 5) * sizeof(Stage);
@@ -417,6 +428,8 @@ __global__ void __launch_bounds__(256, ONE ? 4 : 3) ev_pass(EvArgs a, int pass, 
                     for (uint32_t k = lane; k < (uint32_t)(pool_end - pool_next); k += 32) {
                         uint64_t idx = pool_next + k;
                         if (SOURCE) {
+                            /* the whole birth here, two records per lane, so the
+                               per-lane hand-out below is a copy */
                             uint32_t inst = 0;
                             if (!ONE) {
                                 uint32_t lo = 0, hi = a.n_inst;
@@ -427,26 +440,57 @@ __global__ void __launch_bounds__(256, ONE ? 4 : 3) ev_pass(EvArgs a, int pass, 
                                 inst = lo;
                             }
                             const EvInst& I = a.inst[inst];
-                            uint32_t local = (uint32_t)(idx - I.hist_begin);
-                            uint4 rec4 = make_uint4(0u, 0xFFFFFFFFu, inst, local);   /* fresh source */
+                            /* the record's instance, not this lane's particle's:
+                               a separate cache from s_hot, which describes the
+                               particle the lane is flying */
+                            unsigned long long gseed, hb;
+                            if (ONE) {
+                                gseed = s_hot[0].gseed;
+                                hb = s_hot[0].hist_begin;
+                            } else {
+                                PfHot& ph = s_pf[threadIdx.x];
+                                if (ph.inst != inst) {
+                                    ph.gseed = nr_generation_seed(I.seed, I.st->gen);
+                                    ph.hist_begin = I.hist_begin;
+                                    ph.inst = inst;
+                                }
+                                gseed = ph.gseed;
+                                hb = ph.hist_begin;
+                            }
+                            const uint32_t local = (uint32_t)(idx - hb);
+                            nr_pcg32 rng = nr_pcg32_seeded(gseed, local);
+                            float bx = 0.0f, bmu;
+                            uint32_t bg = 0;
+                            bool banked = false;
                             if (BANK && ONE) {
                                 if (s_src.nbk > 0) {
                                     /* one 16-byte load of the site (x, cell, group, pad) */
-                                    uint4 sv = reinterpret_cast<const uint4*>(s_src.bank)[bank_site(local, s_src.nbk, s_src.ndiv)];
-                                    rec4.x = sv.x;
-                                    rec4.y = sv.z;
+                                    const uint4 sv = reinterpret_cast<const uint4*>(s_src.bank)[bank_site(local, s_src.nbk, s_src.ndiv)];
+                                    bx = __uint_as_float(sv.x); bg = sv.z; banked = true;
                                 }
                             } else if (BANK) {
                                 const GenState* st = I.st;
-                                uint64_t nbk = st->n_bank;
+                                const uint64_t nbk = st->n_bank;
                                 if (nbk > 0) {
                                     const nraps_site* bank = I.bank[st->gen & 1];
-                                    uint4 sv = reinterpret_cast<const uint4*>(bank)[bank_site(local, nbk, I.ndiv)];
-                                    rec4.x = sv.x;
-                                    rec4.y = sv.z;
+                                    const uint4 sv = reinterpret_cast<const uint4*>(bank)[bank_site(local, nbk, I.ndiv)];
+                                    bx = __uint_as_float(sv.x); bg = sv.z; banked = true;
                                 }
                             }
-                            sg.pf_a[k] = rec4;
+                            if (banked) {
+                                bmu = __fsub_rn(__fmul_rn(2.0f, u24(nr_pcg32_next(&rng))), 1.0f);
+                            } else {
+                                /* fresh uniform fuel source (spawn_neutron) */
+                                const uint32_t cell = I.fuel[((uint64_t)nr_pcg32_next(&rng) * I.nfuel) >> 32];
+                                const float sub = u24(nr_pcg32_next(&rng));
+                                bx = __fadd_rn(I.cleft[cell], __fmul_rn(sub, I.cdx[cell]));
+                                bmu = __fsub_rn(__fmul_rn(2.0f, u24(nr_pcg32_next(&rng))), 1.0f);
+                                bg = count_below(I.chicdf + (uint32_t)I.cmat[cell] * I.G, I.G, u24(nr_pcg32_next(&rng)));
+                            }
+                            if (REC && inst == 0) a.rec[local].draws += banked ? 1 : 4;
+                            sg.pf_a[k] = make_uint4(__float_as_uint(bx), __float_as_uint(bmu), (uint32_t)idx,
+                                                    bg | (inst << 4));
+                            sg.pf_rng[k] = rng.state;
                         } else {
                             sg.pf_a[k] = make_uint4(__float_as_uint(a.qx[qin][idx]), __float_as_uint(a.qmu[qin][idx]),
                                                     a.qid[qin][idx], a.qpk[qin][idx]);
@@ -464,42 +508,20 @@ __global__ void __launch_bounds__(256, ONE ? 4 : 3) ev_pass(EvArgs a, int pass, 
             uint32_t n_need = __popc(need);
             pool_next += (uint64_t)n_need < avail ? n_need : avail;
             if (got) {
-                uint4 r4 = sg.pf_a[slot];
-                if (SOURCE) {
-                    uint32_t inst = r4.z;
-                    Hot& h = s_hot[ONE ? 0 : threadIdx.x];
-                    if (!ONE && h.inst != inst) load_hot(h, a.inst[inst], inst, BANK);
-                    p.inst = inst;
-                    p.local = r4.w;
-                    p.id = (uint32_t)(h.hist_begin + p.local);
-                    p.seq = 0;
-                    p.rng = nr_pcg32_seeded(h.gseed, p.local);
-                    if (r4.y != 0xFFFFFFFFu) {
-                        p.x = __uint_as_float(r4.x); p.g = r4.y;
-                        p.mu = __fsub_rn(__fmul_rn(2.0f, u24(nr_pcg32_next(&p.rng))), 1.0f);
-                    } else {
-                        const EvInst& I = a.inst[inst];
-                        uint32_t cell = I.fuel[((uint64_t)nr_pcg32_next(&p.rng) * I.nfuel) >> 32];
-                        float sub = u24(nr_pcg32_next(&p.rng));
-                        p.x = __fadd_rn(I.cleft[cell], __fmul_rn(sub, I.cdx[cell]));
-                        p.mu = __fsub_rn(__fmul_rn(2.0f, u24(nr_pcg32_next(&p.rng))), 1.0f);
-                        p.g = count_below(I.chicdf + (uint32_t)I.cmat[cell] * I.G, I.G, u24(nr_pcg32_next(&p.rng)));
-                    }
-                    if (REC && inst == 0) a.rec[p.local].draws += (r4.y != 0xFFFFFFFFu) ? 1 : 4;
-                } else {
-                    p.x = __uint_as_float(r4.x);
-                    p.mu = __uint_as_float(r4.y);
-                    p.id = r4.z;
-                    uint32_t pk = r4.w;
-                    p.rng.state = sg.pf_rng[slot];
-                    p.g = pk & 15u;
-                    p.inst = ONE ? 0u : (pk >> 4) & 0xFFFu;
-                    p.seq = pk >> 16;
-                    Hot& h = s_hot[ONE ? 0 : threadIdx.x];
-                    if (!ONE && h.inst != p.inst) load_hot(h, a.inst[p.inst], p.inst, BANK);
-                    p.local = (uint32_t)(p.id - h.hist_begin);
-                    p.rng.inc = ((uint64_t)p.local << 1) | 1ULL;
-                }
+                /* birth record or queue entry: same layout */
+                const uint4 r4 = sg.pf_a[slot];
+                p.x = __uint_as_float(r4.x);
+                p.mu = __uint_as_float(r4.y);
+                p.id = r4.z;
+                const uint32_t pk = r4.w;
+                p.rng.state = sg.pf_rng[slot];
+                p.g = pk & 15u;
+                p.inst = ONE ? 0u : (pk >> 4) & 0xFFFu;
+                p.seq = pk >> 16;
+                Hot& h = s_hot[ONE ? 0 : threadIdx.x];
+                if (!ONE && h.inst != p.inst) load_hot(h, a.inst[p.inst], p.inst, BANK);
+                p.local = (uint32_t)(p.id - h.hist_begin);
+                p.rng.inc = ((uint64_t)p.local << 1) | 1ULL;
                 Ip = &a.inst[ONE ? 0 : p.inst];
                 if (!ONE && p.inst != tv_inst) {
                     tv = global_view(*Ip);
@@ -552,6 +574,10 @@ __global__ void __launch_bounds__(256, ONE ? 4 : 3) ev_pass(EvArgs a, int pass, 
         bool real = false;
         uint32_t m = 0, cell = 0, pending = 0;
         if (have) {
+            /* one flight per step: a virtual collision ends the lane's step,
+               so the next flight runs converged with the other lanes' flights
+               (looping over virtual collisions here measured 30% more
+               instructions: the extra iterations run divergent) */
             if (++events > a.max_events) {
                 fate = NRAPS_FATE_CAPPED;
             } else {

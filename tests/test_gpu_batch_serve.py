@@ -26,6 +26,29 @@ def instances(n, seed=5, inactive=4, active=6):
     return out
 
 
+def test_many_small_instances_equal_alone(ctx_factory):
+    """Many small instances whose sizes are not multiples of the 64-particle
+    claim: nearly every chunk a warp takes spans two instances, so a lane
+    prefetches records of one instance while flying a particle of another."""
+    rng = np.random.default_rng(11)
+    probs = []
+    for _ in range(24):
+        R = int(rng.integers(3, 10))
+        G = int(rng.integers(2, 7))
+        N = int(rng.integers(300, 1500))
+        probs.append(synth.random_slab(rng, R, G, 0.5, 3.0, 10, N, 3, 4))
+    seeds = [500 + i for i in range(len(probs))]
+    ctx = ctx_factory(seed=1, **WC)
+    b = api.Batch(ctx, probs, seeds=seeds)
+    b.run(probs[0].generations)
+    for i, p in enumerate(probs):
+        r = b.results(i)
+        alone = ctx_factory(seed=seeds[i], **WC).solve(p)
+        assert np.array_equal(r.k64, alone.k64), i
+        np.testing.assert_allclose(r.flux_mean, alone.flux_mean, rtol=1e-9, atol=0)
+    b.close()
+
+
 def test_batch_equals_each_instance_alone(ctx_factory):
     probs = instances(5)
     seeds = [101 + i for i in range(len(probs))]
