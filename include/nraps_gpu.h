@@ -419,12 +419,34 @@ int nraps_format_f64(double v, char* buf, uint64_t cap);
 int nraps_write_solution(const char* dir, const nraps_result* r, uint32_t energygroups,
                          uint64_t cells, uint64_t generations, double assembly_length);
 /* The dispatch of src/main.rs:332-364: process_input(input_path; NULL =
-   "./TestCaseC.txt"), mesh_gen, Monte Carlo with k = 1.0 on ctx when the
-   file has Solution = 1, then nraps_write_solution into out_dir with the
-   last cell's right edge as the assembly length.  Other Solution values
-   select the deterministic solvers: NRAPS_ERR_UNSUPPORTED.  stats_out may be
-   NULL. */
+   "./TestCaseC.txt"), mesh_gen, then
+     Solution = 1           -> Monte Carlo with k = 1.0 on ctx;
+     otherwise, solver LinAlg -> nraps_diffusion_solve (no GPU; ctx may be
+                               NULL), whose results have one k, no k_fund
+                               and no fission source: those CSV rows are
+                               written empty;
+     other solvers          -> NRAPS_ERR_UNSUPPORTED (the reference returns
+                               empty results for them);
+   then the three CSV files into out_dir with the last cell's right edge as
+   the assembly length.  stats_out (Monte Carlo only) may be NULL. */
 int nraps_run_input(nraps_ctx* ctx, const char* input_path, const char* out_dir, nraps_stats* stats_out);
+
+/* ---- deterministic diffusion solver (no GPU) -----------------------------
+   nalgebra_method (src/discrete.rs:169-356): multigroup finite-difference
+   diffusion with the reference's boundary rows, group sweep, convergence
+   test (delta_flux >= 1e-5 and delta_k >= 1e-6 keep it going) and power
+   normalisation, in FP64 with tridiagonal solves (agrees with the reference
+   to its f32 rounding).  flux / assembly_average: caller-allocated G*cells
+   f32 or NULL.  max_iterations 0 = 100000; NRAPS_ERR_CAPPED if reached. */
+typedef struct nraps_diffusion_info {
+    double   k;
+    uint64_t iterations;
+    int32_t  converged;
+    int32_t  pad;
+    double   delta_flux, delta_k;
+} nraps_diffusion_info;
+int nraps_diffusion_solve(const nraps_problem* problem, uint64_t max_iterations, float* flux,
+                          float* assembly_average, nraps_diffusion_info* info);
 
 /* Text of a status code. */
 const char* nraps_status_string(int status);

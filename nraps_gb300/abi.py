@@ -112,6 +112,11 @@ class Problem(C.Structure):
                 ("k_new", C.c_float)]
 
 
+class DiffusionInfo(C.Structure):
+    _fields_ = [("k", C.c_double), ("iterations", C.c_uint64), ("converged", C.c_int32), ("pad", C.c_int32),
+                ("delta_flux", C.c_double), ("delta_k", C.c_double)]
+
+
 class Stats(C.Structure):
     _fields_ = [
         ("k_mean", C.c_double), ("k_sigma", C.c_double),

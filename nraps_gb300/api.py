@@ -108,6 +108,8 @@ def load(build_if_missing: bool = True):
     L.nraps_write_solution.argtypes = [C.c_char_p, P(abi.Result), C.c_uint32, C.c_uint64, C.c_uint64,
                                        C.c_double]
     L.nraps_run_input.argtypes = [vp, C.c_char_p, C.c_char_p, P(abi.Stats)]
+    L.nraps_diffusion_solve.argtypes = [P(abi.Problem), C.c_uint64, P(C.c_float), P(C.c_float),
+                                        P(abi.DiffusionInfo)]
     L.nraps_status_string.argtypes = [C.c_int]
     L.nraps_status_string.restype = C.c_char_p
     _LIB = L
@@ -249,6 +251,32 @@ def write_solution(res: ResultArrays, generations: int, assembly_length: float, 
     rv = res.view()
     _check(L.nraps_write_solution(out_dir.encode(), C.byref(rv), res.G, res.cells, generations,
                                   float(assembly_length)))
+
+
+def diffusion_solve(prob: ProblemArrays, max_iterations: int = 0):
+    """nalgebra_method (src/discrete.rs:169-356) on the host: returns
+    (flux[G, cells], assembly_average[G, cells], info dict)."""
+    L = load()
+    G, n = prob.energygroups, prob.n_cells
+    flux = np.zeros(G * n, np.float32)
+    avg = np.zeros(G * n, np.float32)
+    info = abi.DiffusionInfo()
+    pv = prob.view()
+    _check(L.nraps_diffusion_solve(C.byref(pv), max_iterations, flux.ctypes.data_as(C.POINTER(C.c_float)),
+                                   avg.ctypes.data_as(C.POINTER(C.c_float)), C.byref(info)))
+    return (flux.reshape(G, n), avg.reshape(G, n),
+            dict(k=info.k, iterations=info.iterations, converged=bool(info.converged),
+                 delta_flux=info.delta_flux, delta_k=info.delta_k))
+
+
+def run_input(input_path: str = "./TestCaseC.txt", out_dir: str = ".", ctx: "Context | None" = None):
+    """The restored main dispatch without a context: only input files that
+    select the deterministic solver run (Monte Carlo needs a Context)."""
+    L = load()
+    st = abi.Stats()
+    h = ctx.h if ctx is not None else None
+    _check(L.nraps_run_input(h, input_path.encode(), out_dir.encode(), C.byref(st)), h)
+    return st
 
 
 # ------------------------------------------------------------------ solver --

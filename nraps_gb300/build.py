@@ -39,7 +39,7 @@ CU_SOURCES = {
     "noalloc.cu": ["--fmad=false"],
     "serve.cu": [],
 }
-CPP_SOURCES = ["host_frontend.cpp", "host_output.cpp", "tables.cpp"]
+CPP_SOURCES = ["host_frontend.cpp", "host_output.cpp", "host_diffusion.cpp", "tables.cpp"]
 CLI_SOURCE = "nraps_main.cpp"  # the `nraps` program, linked against the library
 
 

@@ -99,7 +99,7 @@ struct File {
 };
 
 void write_row(std::string& out, const float* v, uint64_t n) {
-    for (uint64_t i = 0; i < n; ++i) {
+    for (uint64_t i = 0; i < n && v; ++i) {
         if (i) out.push_back(',');
         out += rust_display(v[i]);
     }
@@ -127,6 +127,37 @@ int nraps_format_f32(float v, char* buf, uint64_t cap) { return put(rust_display
 
 int nraps_format_f64(double v, char* buf, uint64_t cap) { return put(rust_display(v), buf, cap); }
 
+}  /* extern "C" */
+
+namespace {
+
+/* plot_solution's three files; the row lengths are the results' own
+   (the deterministic solver has one k and no k_fund or fission source) */
+int write_files(const char* dir, uint32_t G, uint64_t cells, uint64_t generations, double length,
+                const float* flux, const float* avg, const float* fis, uint64_t n_fis, const float* k,
+                uint64_t n_k, const float* k_fund, uint64_t n_kf) {
+    std::string vars;
+    vars += rust_display(length) + "\n";
+    vars += std::to_string(cells) + "\n";
+    vars += std::to_string(generations) + "\n";
+    std::string iface;
+    iface.reserve((size_t)(2 * G + 1) * cells * 12);
+    for (uint32_t g = 0; g < G; ++g) write_row(iface, flux + (uint64_t)g * cells, cells);
+    for (uint32_t g = 0; g < G; ++g) write_row(iface, avg + (uint64_t)g * cells, cells);
+    write_row(iface, fis, n_fis);
+    std::string keff;
+    write_row(keff, k, n_k);
+    write_row(keff, k_fund, n_kf);
+    int s;
+    if ((s = write_file(join_path(dir, "vars.csv"), vars)) != NRAPS_OK) return s;
+    if ((s = write_file(join_path(dir, "interface.csv"), iface)) != NRAPS_OK) return s;
+    return write_file(join_path(dir, "k_eff.csv"), keff);
+}
+
+}  // namespace
+
+extern "C" {
+
 int nraps_write_solution(const char* dir, const nraps_result* r, uint32_t energygroups, uint64_t cells,
                          uint64_t generations, double assembly_length) {
     /* plot_solution indexes results.flux[0] and results.assembly_average[0]
@@ -137,41 +168,33 @@ int nraps_write_solution(const char* dir, const nraps_result* r, uint32_t energy
         nraps_host::set_error("nraps_write_solution: missing results or zero energy groups");
         return NRAPS_ERR_INVALID;
     }
-    std::string vars;
-    vars += rust_display(assembly_length) + "\n";
-    vars += std::to_string(cells) + "\n";
-    vars += std::to_string(generations) + "\n";
-    std::string iface;
-    iface.reserve((size_t)(2 * energygroups + 1) * cells * 12);
-    for (uint32_t g = 0; g < energygroups; ++g) write_row(iface, r->flux + (uint64_t)g * cells, cells);
-    for (uint32_t g = 0; g < energygroups; ++g) write_row(iface, r->assembly_average + (uint64_t)g * cells, cells);
-    write_row(iface, r->fission_source, cells);
-    std::string keff;
-    write_row(keff, r->k, generations);
-    write_row(keff, r->k_fund, generations);
-    int s;
-    if ((s = write_file(join_path(dir, "vars.csv"), vars)) != NRAPS_OK) return s;
-    if ((s = write_file(join_path(dir, "interface.csv"), iface)) != NRAPS_OK) return s;
-    return write_file(join_path(dir, "k_eff.csv"), keff);
+    return write_files(dir, energygroups, cells, generations, assembly_length, r->flux, r->assembly_average,
+                       r->fission_source, cells, r->k, generations, r->k_fund, generations);
 }
 
 int nraps_run_input(nraps_ctx* ctx, const char* input_path, const char* out_dir, nraps_stats* stats_out) {
-    if (!ctx) {
-        nraps_host::set_error("nraps_run_input: null context");
-        return NRAPS_ERR_INVALID;
-    }
     /* front-end failures are recorded per thread; move them onto the context */
     auto host_fail = [ctx](int code) {
-        nraps_host::set_ctx_error(ctx, nraps_host::last_error());
+        if (ctx) nraps_host::set_ctx_error(ctx, nraps_host::last_error());
+        return code;
+    };
+    auto fail = [ctx](int code, const char* msg) {
+        nraps_host::set_ctx_error(ctx, msg);
         return code;
     };
     nraps_input* in = nullptr;
     int s = nraps_process_input(input_path ? input_path : "./TestCaseC.txt", &in);
     if (s != NRAPS_OK) return host_fail(s);
-    if (in->solution != 0) {
+    const bool monte_carlo = in->solution == 0;
+    if (!monte_carlo && in->solver != 0) {
         nraps_input_free(in);
-        nraps_host::set_ctx_error(ctx, "Solution != 1 selects a deterministic solver, which this library does not carry");
-        return NRAPS_ERR_UNSUPPORTED;
+        return fail(NRAPS_ERR_UNSUPPORTED,
+                    "Solution != 1 with the Gaussian, Jacobian or SR solver: the reference implements "
+                    "only LinAlg (nalgebra_method) and returns empty results for the others");
+    }
+    if (monte_carlo && !ctx) {
+        nraps_input_free(in);
+        return fail(NRAPS_ERR_INVALID, "nraps_run_input: Solution = 1 runs Monte Carlo and needs a context");
     }
     nraps_meshbuf* mesh = nullptr;
     s = nraps_mesh_gen(in->matid, in->n_matid, &in->variables, &in->delta_x, &mesh);
@@ -182,6 +205,29 @@ int nraps_run_input(nraps_ctx* ctx, const char* input_path, const char* out_dir,
     nraps_problem p;
     s = nraps_problem_view(in, mesh, &p);
     if (s != NRAPS_OK) host_fail(s);
+    if (s == NRAPS_OK && !monte_carlo) {
+        /* (_, Solver::LinAlg) => nalgebra_method (src/main.rs:340-348) */
+        const uint64_t G = in->variables.energygroups, nc = mesh->n_cells;
+        std::vector<float> flux(G * nc), avg(G * nc);
+        nraps_diffusion_info info{};
+        s = nraps_diffusion_solve(&p, 0, flux.data(), avg.data(), &info);
+        if (s != NRAPS_OK) {
+            host_fail(s);
+        } else {
+            const float k1 = (float)info.k;
+            if (stats_out) {
+                std::memset(stats_out, 0, sizeof *stats_out);
+                stats_out->k_mean = (double)k1;   /* the solver's one k; no histories */
+            }
+            const double length = (double)mesh->mesh_right[nc - 1];
+            s = write_files(out_dir, (uint32_t)G, nc, in->variables.generations, length, flux.data(), avg.data(),
+                            nullptr, 0, &k1, 1, nullptr, 0);
+            if (s != NRAPS_OK) host_fail(s);
+        }
+        nraps_meshbuf_free(mesh);
+        nraps_input_free(in);
+        return s;
+    }
     const uint64_t G = in->variables.energygroups, nc = mesh->n_cells, gens = in->variables.generations;
     std::vector<float> flux(G * nc), avg(G * nc), fis(nc), k(gens), kf(gens);
     nraps_stats st{};

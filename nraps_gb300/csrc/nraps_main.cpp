@@ -3,8 +3,9 @@
  * reference's main (src/main.rs:332-369) with the Monte Carlo dispatch
  * restored.  It reads an input file (default ./TestCaseC.txt, the file the
  * reference opens at src/process_input.rs:86), runs the Monte Carlo solver
- * when the file says Solution = 1, writes vars.csv, interface.csv and
- * k_eff.csv, and prints the run time in milliseconds.
+ * when the file says Solution = 1 and the deterministic diffusion solver
+ * (LinAlg) otherwise, writes vars.csv, interface.csv and k_eff.csv, and
+ * prints the run time in milliseconds.
  *
  *   nraps [input] [-o out_dir] [--mode compat|physics|bank]
  *         [--form plain|event] [--fp32] [--seed N] [--device N]
@@ -76,12 +77,24 @@ int main(int argc, char** argv) {
         }
     }
     auto t0 = std::chrono::steady_clock::now();
-    nraps_ctx* ctx = nullptr;
-    int s = nraps_create(&ctx, &o);
+    /* a GPU context only for Monte Carlo inputs (Solution = 1) */
+    nraps_input* probe = nullptr;
+    int s = nraps_process_input(input.c_str(), &probe);
     if (s != NRAPS_OK) {
         const char* m = nraps_last_error(nullptr);
         std::fprintf(stderr, "nraps: %s\n", (m && *m) ? m : nraps_status_string(s));
         return 1;
+    }
+    const bool monte_carlo = probe->solution == 0;
+    nraps_input_free(probe);
+    nraps_ctx* ctx = nullptr;
+    if (monte_carlo) {
+        s = nraps_create(&ctx, &o);
+        if (s != NRAPS_OK) {
+            const char* m = nraps_last_error(nullptr);
+            std::fprintf(stderr, "nraps: %s\n", (m && *m) ? m : nraps_status_string(s));
+            return 1;
+        }
     }
     nraps_stats st;
     std::memset(&st, 0, sizeof st);
@@ -89,12 +102,13 @@ int main(int argc, char** argv) {
     if (s != NRAPS_OK) {
         const char* m = nraps_last_error(ctx);
         std::fprintf(stderr, "nraps: %s\n", (m && *m) ? m : nraps_status_string(s));
-        nraps_destroy(ctx);
+        if (ctx) nraps_destroy(ctx);
         return 1;
     }
-    nraps_destroy(ctx);
+    if (ctx) nraps_destroy(ctx);
     auto ms = std::chrono::duration_cast<std::chrono::milliseconds>(std::chrono::steady_clock::now() - t0).count();
     std::printf("Run was completed in %lld milliseconds \n", (long long)ms);
-    std::printf("k = %.6f +- %.6f over the active generations\n", st.k_mean, st.k_sigma);
+    if (st.histories) std::printf("k = %.6f +- %.6f over the active generations\n", st.k_mean, st.k_sigma);
+    else std::printf("%.10f\n", st.k_mean);   /* nalgebra_method prints its k ({:.10}) */
     return 0;
 }

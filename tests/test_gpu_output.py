@@ -73,10 +73,11 @@ def test_run_input_compat_default(ctx_factory, tmp_path):
 
 def test_run_input_dispatch_errors(ctx_factory, tmp_path):
     ctx = ctx_factory(seed=1)
-    with pytest.raises(api.NrapsError) as e:
-        ctx.run_input(os.path.join(INPUTS, "TestCaseA.txt"), str(tmp_path))  # Solution = 0
-    assert e.value.status == abi.ERR_UNSUPPORTED
-    assert "deterministic" in str(e.value)
+    # Solution = 0 with the LinAlg solver: the deterministic solver, one k
+    det = tmp_path / "det"
+    det.mkdir()
+    ctx.run_input(os.path.join(INPUTS, "TestCaseA.txt"), str(det))
+    assert len(open(det / "k_eff.csv").read().split("\n")[0].split(",")) == 1
     with pytest.raises(api.NrapsError) as e:
         ctx.run_input(str(tmp_path / "missing.txt"), str(tmp_path))
     assert e.value.status == abi.ERR_IO
@@ -93,6 +94,8 @@ def test_cli_program(tmp_path):
     assert "Run was completed in" in r.stdout
     for name in ("vars.csv", "interface.csv", "k_eff.csv"):
         assert (tmp_path / name).exists()
-    r = subprocess.run([CLI, os.path.join(INPUTS, "TestCaseB.txt"), "-o", str(tmp_path)],
+    text = open(os.path.join(INPUTS, "TestCaseB.txt")).read().replace("solver   = 0", "solver   = 3")
+    (tmp_path / "sr.txt").write_text(text)
+    r = subprocess.run([CLI, str(tmp_path / "sr.txt"), "-o", str(tmp_path)],
                        capture_output=True, text=True, timeout=300)
-    assert r.returncode == 1 and "deterministic" in r.stderr
+    assert r.returncode == 1 and "LinAlg" in r.stderr
