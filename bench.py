@@ -155,7 +155,7 @@ ARMS = {
 }
 
 
-def measure_device(prob, arm: str, steps: int, warmup: int, seed: int, device: int, shape=None):
+def measure_device(prob, arm: str, steps: int, warmup: int, seed: int, device: int, shape=None, pool=0):
     """Device-resident throughput: per-step CUDA events on the engine stream.
     shape = (block, events_per_pass, passes[, tail_lanes]) fixes the event launch shape
     (no autotuning); None lets the engine tune it over the warm-up."""
@@ -166,6 +166,8 @@ def measure_device(prob, arm: str, steps: int, warmup: int, seed: int, device: i
         kw.update(block_size=shape[0], events_per_pass=shape[1], passes=shape[2])
         if len(shape) > 3:
             kw.update(tail_lanes=shape[3])
+    if pool:
+        kw.update(pool_slots=pool)
     ctx = api.Context(seed=seed, device=device, **kw)
     s = ctx.session(prob)
     s.set_profile(True)
@@ -342,6 +344,7 @@ def main():
     ap.add_argument("--serve-rate", type=float, default=200.0)
     ap.add_argument("--shape", type=lambda v: tuple(int(x) for x in v.split(",")), default=None,
                     help="block,events_per_pass,passes[,tail_lanes]: fixed event launch shape (profiling)")
+    ap.add_argument("--pool", type=int, default=0, help="pool transport with this many slots per block (profiling)")
     ap.add_argument("--scale-stress", type=int, default=1, help="1 = also run the 10M-history, 200k-cell slab")
     args = ap.parse_args()
     if args.warmup < 3:
@@ -375,7 +378,7 @@ def main():
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
-    d = measure_device(prob, arm, args.steps, args.warmup, seed, local, shape=args.shape)
+    d = measure_device(prob, arm, args.steps, args.warmup, seed, local, shape=args.shape, pool=args.pool)
     clk = clocks.stop()
     ms = max_over_ranks(d["ms"], f"cuda:{local}")
     if world > 1:

@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define NRAPS_ABI_VERSION 2u
+#define NRAPS_ABI_VERSION 3u
 
 /* ---- status codes ------------------------------------------------------- */
 #define NRAPS_OK              0
@@ -98,7 +98,12 @@ typedef struct nraps_opts {
                                     warp with fewer live particles re-queues
                                     them for the next pass (needs passes >= 1);
                                     0 = off                                   */
-    uint32_t reserved[5];
+    uint32_t pool_slots;         /* WOODCOCK, one instance: > 0 = the pool
+                                    transport (particles kept in shared memory,
+                                    advanced in block-wide phases over
+                                    compacted lists) with this many slots per
+                                    block, 64..4096; 0 = tuned                */
+    uint32_t reserved[4];
 } nraps_opts;
 
 /* Fill *o with the defaults (FP64 surface tracking, COMPAT, seed 1). */
@@ -247,8 +252,8 @@ int  nraps_session_timing(nraps_session* s, double* transport_ms, double* total_
    is kept; results do not depend on the shape.  tried_ms receives the
    transport time of each candidate tried (up to tried_cap). */
 int  nraps_session_tuning(nraps_session* s, uint32_t* block, uint32_t* events_per_pass,
-                          uint32_t* passes, uint32_t* tail_lanes, uint32_t* n_tried, float* tried_ms,
-                          uint32_t tried_cap);
+                          uint32_t* passes, uint32_t* tail_lanes, uint32_t* pool_slots, uint32_t* n_tried,
+                          float* tried_ms, uint32_t tried_cap);
 /* generations completed so far (enqueued work included after sync) */
 uint64_t nraps_session_generation(const nraps_session* s);
 void nraps_session_destroy(nraps_session* s);

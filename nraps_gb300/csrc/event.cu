@@ -258,6 +258,41 @@ __host__ __device__ __forceinline__ size_t smem_bytes_for(uint32_t M, uint32_t G
     return (b + 15) / 16 * 16;
 }
 
+/* Copies one instance's tables into shared memory at tab (block-wide; the
+   caller synchronises) and points t at them. */
+__device__ __forceinline__ void stage_tables(const EvInst& I, unsigned char* tab, TView& t) {
+    const uint32_t M = I.M, G = I.G, R = I.R, NB = I.nbins;
+    double* s_inv64 = reinterpret_cast<double*>(tab);
+    unsigned long long* s_kq = reinterpret_cast<unsigned long long*>(s_inv64 + M * G);
+    float* f = reinterpret_cast<float*>(s_kq + M * G);
+    float* s_xs = f;                 f += M * G * 4;
+    float* s_scdf = f;               f += M * G * G;
+    float* s_chi = f;                f += M * G;
+    float* s_maj = f;                f += 2 * G;
+    float* s_left = f;               f += R + 1;
+    float* s_invdx = f;              f += R;
+    uint32_t* s_first = reinterpret_cast<uint32_t*>(f);  f += R;
+    uint32_t* s_ncell = reinterpret_cast<uint32_t*>(f);  f += R;
+    uint16_t* s_grid = reinterpret_cast<uint16_t*>(f);
+    uint8_t* s_rmat = reinterpret_cast<uint8_t*>(s_grid + NB);
+    for (uint32_t i = threadIdx.x; i < M * G; i += blockDim.x) { s_inv64[i] = I.inv_st64[i]; s_kq[i] = I.kq[i]; }
+    for (uint32_t i = threadIdx.x; i < M * G * 4; i += blockDim.x) s_xs[i] = I.xs[i];
+    for (uint32_t i = threadIdx.x; i < M * G * G; i += blockDim.x) s_scdf[i] = I.scdf[i];
+    for (uint32_t i = threadIdx.x; i < M * G; i += blockDim.x) s_chi[i] = I.chicdf[i];
+    for (uint32_t i = threadIdx.x; i < 2 * G; i += blockDim.x) s_maj[i] = I.maj[i];
+    for (uint32_t i = threadIdx.x; i < R + 1; i += blockDim.x) s_left[i] = I.rleft[i];
+    for (uint32_t i = threadIdx.x; i < R; i += blockDim.x) {
+        s_invdx[i] = I.rinvdx[i]; s_first[i] = I.rfirst[i]; s_ncell[i] = I.rncell[i];
+    }
+    for (uint32_t i = threadIdx.x; i < NB; i += blockDim.x) s_grid[i] = I.grid[i];
+    for (uint32_t i = threadIdx.x; i < R; i += blockDim.x) s_rmat[i] = I.rmat[i];
+    t.xs = s_xs; t.inv_st64 = s_inv64; t.kq = s_kq; t.scdf = s_scdf; t.chi = s_chi; t.maj = s_maj;
+    t.left = s_left; t.grid = s_grid; t.rmat = s_rmat; t.invdx = s_invdx; t.first = s_first;
+    t.ncell = s_ncell;
+    t.G = G; t.R = R; t.nbins = NB; t.L = I.L; t.inv_binw = I.inv_binw;
+    t.boundl = I.boundl; t.boundr = I.boundr;
+}
+
 constexpr int WARPS_MAX = 8;        /* blocks of at most 256 threads          */
 struct Stage;
 __host__ __device__ __forceinline__ size_t stage_bytes(uint32_t block);
@@ -295,7 +330,8 @@ __device__ __forceinline__ void flush_particles(const EvArgs& a, Stage& sg, uint
 
 /* flush the first n staged sites of a warp into its slab (warp-wide);
    returns false (all lanes) if the slab is full */
-__device__ __forceinline__ bool flush_sites(const EvArgs& a, Stage& sg, uint32_t n, uint32_t slab,
+template <class S>
+__device__ __forceinline__ bool flush_sites(const EvArgs& a, S& sg, uint32_t n, uint32_t slab,
                                             uint32_t lane) {
     unsigned long long base = 0;
     if (lane == 0) base = atomicAdd(&a.slab_count[slab], (unsigned long long)n);
@@ -351,37 +387,8 @@ __global__ void __launch_bounds__(256, ONE ? 4 : 3) ev_pass(EvArgs a, int pass, 
                 s_src.ndiv = I.ndiv;
             }
         }
-        const uint32_t M = I.M, G = I.G, R = I.R, NB = I.nbins;
-        double* s_inv64 = reinterpret_cast<double*>(tab);
-        unsigned long long* s_kq = reinterpret_cast<unsigned long long*>(s_inv64 + M * G);
-        float* f = reinterpret_cast<float*>(s_kq + M * G);
-        float* s_xs = f;                 f += M * G * 4;
-        float* s_scdf = f;               f += M * G * G;
-        float* s_chi = f;                f += M * G;
-        float* s_maj = f;                f += 2 * G;
-        float* s_left = f;               f += R + 1;
-        float* s_invdx = f;              f += R;
-        uint32_t* s_first = reinterpret_cast<uint32_t*>(f);  f += R;
-        uint32_t* s_ncell = reinterpret_cast<uint32_t*>(f);  f += R;
-        uint16_t* s_grid = reinterpret_cast<uint16_t*>(f);
-        uint8_t* s_rmat = reinterpret_cast<uint8_t*>(s_grid + NB);
-        for (uint32_t i = threadIdx.x; i < M * G; i += blockDim.x) { s_inv64[i] = I.inv_st64[i]; s_kq[i] = I.kq[i]; }
-        for (uint32_t i = threadIdx.x; i < M * G * 4; i += blockDim.x) s_xs[i] = I.xs[i];
-        for (uint32_t i = threadIdx.x; i < M * G * G; i += blockDim.x) s_scdf[i] = I.scdf[i];
-        for (uint32_t i = threadIdx.x; i < M * G; i += blockDim.x) s_chi[i] = I.chicdf[i];
-        for (uint32_t i = threadIdx.x; i < 2 * G; i += blockDim.x) s_maj[i] = I.maj[i];
-        for (uint32_t i = threadIdx.x; i < R + 1; i += blockDim.x) s_left[i] = I.rleft[i];
-        for (uint32_t i = threadIdx.x; i < R; i += blockDim.x) {
-            s_invdx[i] = I.rinvdx[i]; s_first[i] = I.rfirst[i]; s_ncell[i] = I.rncell[i];
-        }
-        for (uint32_t i = threadIdx.x; i < NB; i += blockDim.x) s_grid[i] = I.grid[i];
-        for (uint32_t i = threadIdx.x; i < R; i += blockDim.x) s_rmat[i] = I.rmat[i];
+        stage_tables(I, tab, t);
         __syncthreads();
-        t.xs = s_xs; t.inv_st64 = s_inv64; t.kq = s_kq; t.scdf = s_scdf; t.chi = s_chi; t.maj = s_maj;
-        t.left = s_left; t.grid = s_grid; t.rmat = s_rmat; t.invdx = s_invdx; t.first = s_first;
-        t.ncell = s_ncell;
-        t.G = G; t.R = R; t.nbins = NB; t.L = I.L; t.inv_binw = I.inv_binw;
-        t.boundl = I.boundl; t.boundr = I.boundr;
     }
     const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const unsigned lt = (1u << lane) - 1u;
@@ -718,6 +725,313 @@ __global__ void __launch_bounds__(256, ONE ? 4 : 3) ev_pass(EvArgs a, int pass, 
         if (ab) atomicAdd(&s->absorbed, ab);
         if (lk) atomicAdd(&s->leaked, lk);
         if (cp) atomicAdd(&s->capped, cp);
+    }
+}
+
+/*
+ * Pool transport (single instance, tables in shared memory, one pass: every
+ * particle runs to its end).  Each block keeps up to P particles in shared
+ * memory as structure-of-arrays and advances them in block-wide phases over
+ * compacted slot lists, so the threads of a phase run the same code:
+ *   refill  births into the free slots (one claim per block per round);
+ *   A       one flight per live particle: distance, boundary, region,
+ *           Woodcock test -> real collisions to list R, virtual ones stay
+ *           live, leaked and capped histories end;
+ *   B       one real collision per particle of R: tally and k scores,
+ *           fission sites, absorption (ends) or scatter (stays live).
+ * In ev_pass a warp executes every path any of its lanes takes, each with
+ * the lanes that take it; here a phase's threads share one path.  A
+ * particle's draws are the same sequence as in ev_pass, so every history,
+ * and every result, is the same as with any other launch shape.
+ */
+constexpr int POOL_THREADS = 256;
+constexpr int POOL_WARPS = POOL_THREADS / 32;
+constexpr uint32_t POOL_MAX = 4096;          /* slot indices are u16 */
+
+struct PoolSite {
+    uint4 site[STAGE];
+};
+
+/* shared memory of the pool (slots, lists, site staging), before the tables */
+__host__ __device__ __forceinline__ size_t pool_bytes(uint32_t P) {
+    size_t b = (size_t)P * (8 + 4 * 6) + (size_t)P * 2 * 4;
+    b = (b + 15) & ~(size_t)15;
+    return b + POOL_WARPS * sizeof(PoolSite);
+}
+
+template <bool EXACT, bool BANK>
+__global__ void __launch_bounds__(POOL_THREADS, 2) ev_pool(EvArgs a, uint32_t P) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ Hot s_h1;
+    __shared__ SrcBank s_src;
+    __shared__ uint32_t s_n[8];             /* live, next live, real, free, births, exhausted */
+    __shared__ unsigned long long s_base;
+    unsigned long long* prng = reinterpret_cast<unsigned long long*>(smem);
+    float* px = reinterpret_cast<float*>(prng + P);
+    float* pmu = px + P;
+    uint32_t* pev = reinterpret_cast<uint32_t*>(pmu + P);
+    uint32_t* pgs = pev + P;                /* group | site sequence << 8 */
+    uint32_t* pid = pgs + P;
+    uint32_t* preg = pid + P;               /* region of the pending real collision */
+    uint16_t* La = reinterpret_cast<uint16_t*>(preg + P);
+    uint16_t* Lb = La + P;
+    uint16_t* Rl = Lb + P;
+    uint16_t* Fl = Rl + P;
+    const size_t lists_end = (((size_t)(reinterpret_cast<unsigned char*>(Fl + P) - smem)) + 15) & ~(size_t)15;
+    PoolSite* s_site = reinterpret_cast<PoolSite*>(smem + lists_end);
+    unsigned char* tab = smem + lists_end + POOL_WARPS * sizeof(PoolSite);
+    const EvInst& I = a.inst[0];
+    if (threadIdx.x == 0) {
+        load_hot(s_h1, I, 0, BANK);
+        if (BANK) {
+            const GenState* st = I.st;
+            s_src.bank = I.bank[st->gen & 1];
+            s_src.nbk = st->n_bank;
+            s_src.ndiv = I.ndiv;
+        }
+        s_n[0] = 0; s_n[1] = 0; s_n[2] = 0; s_n[3] = P; s_n[4] = 0; s_n[5] = 0;
+    }
+    for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) Fl[i] = (uint16_t)i;
+    TView tv;
+    stage_tables(I, tab, tv);
+    __syncthreads();
+    const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const unsigned lt = (1u << lane) - 1u;
+    const unsigned FULL = 0xffffffffu;
+    const uint32_t G = tv.G;
+    PoolSite& sg = s_site[w];
+    const uint32_t slab = (blockIdx.x * POOL_WARPS + w) % NSLAB;
+    uint32_t staged_sites = 0;
+    bool slab_full = false;
+    Acc acc = {0, 0, 0, 0, 0, 0};
+    const float inv_k = s_h1.inv_k;
+    const unsigned long long gseed = s_h1.gseed, hist_begin = s_h1.hist_begin;
+    double* const tally = s_h1.tally;
+    const uint32_t nc = s_h1.nc;
+    const uint64_t n_in = a.n_total;
+    uint16_t* L = La;
+    uint16_t* Ln = Lb;
+    /* warp-aggregated append of slot s to list `lst` with counter `cnt` */
+    auto append = [&](bool want, uint16_t s, uint16_t* lst, uint32_t* cnt) {
+        const unsigned m = __ballot_sync(FULL, want);
+        if (!m) return;
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(cnt, (uint32_t)__popc(m));
+        base = __shfl_sync(FULL, base, 0);
+        if (want) lst[base + __popc(m & lt)] = s;
+    };
+    /* a history ends: its site count for the bank order, counters */
+    auto end_history = [&](uint32_t id, uint32_t seq, int fate) {
+        if (fate == NRAPS_FATE_ABSORBED) acc.absorbed++;
+        else if (fate == NRAPS_FATE_LEAKED) acc.leaked++;
+        else { acc.capped++; atomicOr(&I.st->error, NR_ERR_CAPPED); }
+        if (BANK) a.count[id] = seq;
+    };
+    for (;;) {
+        /* ---- refill: births into free slots --------------------------------- */
+        if (threadIdx.x == 0) {
+            const uint32_t nf = s_n[3];
+            uint32_t got = 0;
+            unsigned long long base = 0;
+            if (!s_n[5] && nf) {
+                base = atomicAdd(&a.claim[0], (unsigned long long)nf);
+                if (base >= n_in) s_n[5] = 1;
+                else got = (uint32_t)((n_in - base) < nf ? (n_in - base) : nf);
+            }
+            s_base = base;
+            s_n[4] = got;
+        }
+        __syncthreads();
+        {
+            const uint32_t got = s_n[4], nl0 = s_n[0], nf = s_n[3];
+            const unsigned long long base = s_base;
+            for (uint32_t j = threadIdx.x; j < got; j += blockDim.x) {
+                const uint16_t slot = Fl[nf - got + j];
+                const uint64_t idx = base + j;
+                const uint32_t local = (uint32_t)(idx - hist_begin);
+                nr_pcg32 rng = nr_pcg32_seeded(gseed, local);
+                float bx = 0.0f, bmu;
+                uint32_t bg = 0;
+                bool banked = false;
+                if (BANK && s_src.nbk > 0) {
+                    const uint4 sv = reinterpret_cast<const uint4*>(s_src.bank)[bank_site(local, s_src.nbk, s_src.ndiv)];
+                    bx = __uint_as_float(sv.x); bg = sv.z; banked = true;
+                }
+                if (banked) {
+                    bmu = __fsub_rn(__fmul_rn(2.0f, u24(nr_pcg32_next(&rng))), 1.0f);
+                } else {
+                    const uint32_t cell = I.fuel[((uint64_t)nr_pcg32_next(&rng) * I.nfuel) >> 32];
+                    const float sub = u24(nr_pcg32_next(&rng));
+                    bx = __fadd_rn(I.cleft[cell], __fmul_rn(sub, I.cdx[cell]));
+                    bmu = __fsub_rn(__fmul_rn(2.0f, u24(nr_pcg32_next(&rng))), 1.0f);
+                    bg = count_below(I.chicdf + (uint32_t)I.cmat[cell] * I.G, I.G, u24(nr_pcg32_next(&rng)));
+                }
+                px[slot] = bx; pmu[slot] = bmu; prng[slot] = rng.state; pev[slot] = 0;
+                pgs[slot] = bg; pid[slot] = (uint32_t)idx;
+                L[nl0 + j] = slot;
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            s_n[0] += s_n[4];
+            s_n[3] -= s_n[4];
+            s_n[1] = 0;
+            s_n[2] = 0;
+        }
+        __syncthreads();
+        const uint32_t nL = s_n[0];
+        if (nL == 0 && s_n[5]) break;
+        /* ---- A: one flight per live particle -------------------------------- */
+        for (uint32_t b0 = w * 32; b0 < nL; b0 += blockDim.x) {
+            const uint32_t i = b0 + lane;
+            const bool valid = i < nL;
+            const uint16_t s = valid ? L[i] : 0;
+            int out = -1;                   /* 0 live, 1 real, 2 ended */
+            if (valid) {
+                float x = px[s], mu = pmu[s];
+                nr_pcg32 rng;
+                rng.state = prng[s];
+                const uint32_t id = pid[s];
+                rng.inc = ((uint64_t)(uint32_t)(id - hist_begin) << 1) | 1ULL;
+                const uint32_t gs = pgs[s], g = gs & 0xFFu;
+                const uint32_t ev = pev[s] + 1;
+                int fate = -1;
+                if (ev > a.max_events) {
+                    fate = NRAPS_FATE_CAPPED;
+                } else {
+                    const float d = __fmul_rn(neg_log<EXACT>(u24pos(nr_pcg32_next(&rng))), tv.maj[G + g]);
+                    x = __fadd_rn(x, __fmul_rn(mu, d));
+                    int bounce = 0;
+                    while (!(x >= 0.0f && x <= tv.L)) {
+                        if (x > tv.L) {
+                            if (tv.boundr > 0.0f) { x = __fsub_rn(tv.L, __fsub_rn(x, tv.L)); mu = -mu; }
+                            else { fate = NRAPS_FATE_LEAKED; break; }
+                        } else {
+                            if (tv.boundl > 0.0f) { x = -x; mu = -mu; }
+                            else { fate = NRAPS_FATE_LEAKED; break; }
+                        }
+                        if (++bounce > 1000) { fate = NRAPS_FATE_CAPPED; break; }
+                    }
+                    if (fate < 0) {
+                        const uint32_t r = region_of(tv, x);
+                        const uint32_t m = tv.rmat[r];
+                        if (__fmul_rn(u24(nr_pcg32_next(&rng)), tv.maj[g]) < tv.xs[(m * G + g) * 4]) {
+                            out = 1;
+                            preg[s] = r;
+                        } else {
+                            out = 0;
+                            acc.virt++;
+                        }
+                    }
+                }
+                if (fate >= 0) {
+                    out = 2;
+                    end_history(id, gs >> 8, fate);
+                } else {
+                    px[s] = x; pmu[s] = mu; prng[s] = rng.state; pev[s] = ev;
+                }
+            }
+            append(out == 0, s, Ln, &s_n[1]);
+            append(out == 1, s, Rl, &s_n[2]);
+            append(out == 2, s, Fl, &s_n[3]);
+        }
+        __syncthreads();
+        /* ---- B: one real collision per particle of R ------------------------ */
+        const uint32_t nR = s_n[2];
+        for (uint32_t b0 = w * 32; b0 < nR; b0 += blockDim.x) {
+            const uint32_t i = b0 + lane;
+            const bool valid = i < nR;
+            const uint16_t s = valid ? Rl[i] : 0;
+            uint32_t pending = 0, cell = 0, m = 0, g = 0, seq = 0, id = 0;
+            float x = 0.0f;
+            nr_pcg32 rng;
+            rng.state = 0; rng.inc = 1;
+            if (valid) {
+                x = px[s];
+                rng.state = prng[s];
+                id = pid[s];
+                rng.inc = ((uint64_t)(uint32_t)(id - hist_begin) << 1) | 1ULL;
+                const uint32_t gs = pgs[s];
+                g = gs & 0xFFu;
+                seq = gs >> 8;
+                const uint32_t r = preg[s];
+                m = tv.rmat[r];
+                acc.coll++;
+                const float rel = __fmul_rn(__fsub_rn(x, tv.left[r]), tv.invdx[r]);
+                const uint32_t nr = tv.ncell[r];
+                uint32_t k = rel > 0.0f ? (uint32_t)rel : 0u;
+                if (k >= nr) k = nr - 1;
+                cell = tv.first[r] + k;
+                const uint32_t j = m * G + g;
+                nrdev::red_add_f64(&tally[(uint64_t)g * nc + cell], tv.inv_st64[j]);
+                acc.kq += tv.kq[j];
+                if (BANK) {
+                    const float nu = __fadd_rn(__fmul_rn(tv.xs[j * 4 + 2], inv_k), u24(nr_pcg32_next(&rng)));
+                    const int n = (int)floorf(nu);
+                    pending = n > 64 ? 64u : (uint32_t)n;
+                }
+            }
+            if (BANK) {
+                while (__any_sync(FULL, pending > 0)) {
+                    const unsigned sm = __ballot_sync(FULL, pending > 0);
+                    if (pending > 0) {
+                        const uint32_t sgp = count_below(tv.chi + m * G, G, u24(nr_pcg32_next(&rng)));
+                        const uint32_t slot = staged_sites + __popc(sm & lt);
+                        sg.site[slot] = make_uint4(__float_as_uint(x), cell | (sgp << 27), id, seq & 0xFFFFu);
+                        if (seq >= 0xFFFFu) atomicOr(&I.st->error, NR_ERR_CAPACITY);
+                        seq++;
+                        pending--;
+                    }
+                    staged_sites += __popc(sm);
+                    __syncwarp();
+                    if (staged_sites >= 32) {
+                        if (!flush_sites(a, sg, 32, slab, lane)) slab_full = true;
+                        uint4 v = make_uint4(0, 0, 0, 0);
+                        if (lane < staged_sites - 32) v = sg.site[32 + lane];
+                        __syncwarp();
+                        if (lane < staged_sites - 32) sg.site[lane] = v;
+                        __syncwarp();
+                        staged_sites -= 32;
+                    }
+                }
+            }
+            int out = -1;                   /* 0 live, 2 ended */
+            if (valid) {
+                const uint32_t j = m * G + g;
+                if (u24(nr_pcg32_next(&rng)) < tv.xs[j * 4 + 1]) {
+                    out = 2;
+                    end_history(id, seq, NRAPS_FATE_ABSORBED);
+                } else {
+                    const uint32_t ng = count_le(tv.scdf + j * G, G, u24(nr_pcg32_next(&rng)));
+                    pmu[s] = __fsub_rn(__fmul_rn(2.0f, u24(nr_pcg32_next(&rng))), 1.0f);
+                    pgs[s] = ng | (seq << 8);
+                    prng[s] = rng.state;
+                    out = 0;
+                }
+            }
+            append(out == 0, s, Ln, &s_n[1]);
+            append(out == 2, s, Fl, &s_n[3]);
+        }
+        __syncthreads();
+        /* ---- the next live list --------------------------------------------- */
+        uint16_t* t2 = L; L = Ln; Ln = t2;
+        if (threadIdx.x == 0) s_n[0] = s_n[1];
+        __syncthreads();
+    }
+    if (BANK && staged_sites) { if (!flush_sites(a, sg, staged_sites, slab, lane)) slab_full = true; }
+    if (slab_full && lane == 0) atomicOr(&I.st->error, NR_ERR_CAPACITY);
+    unsigned long long kq = nrdev::warp_sum_u64(acc.kq);
+    unsigned long long coll = nrdev::warp_sum_u64(acc.coll), virt = nrdev::warp_sum_u64(acc.virt);
+    unsigned long long ab = nrdev::warp_sum_u64(acc.absorbed), lk = nrdev::warp_sum_u64(acc.leaked);
+    unsigned long long cp = nrdev::warp_sum_u64(acc.capped);
+    if (lane == 0) {
+        GenState* st = a.stats;
+        if (kq) atomicAdd(&I.st->kq, kq);
+        if (coll) atomicAdd(&st->collisions, coll);
+        if (virt) atomicAdd(&st->virtual_collisions, virt);
+        if (ab) atomicAdd(&st->absorbed, ab);
+        if (lk) atomicAdd(&st->leaked, lk);
+        if (cp) atomicAdd(&st->capped, cp);
     }
 }
 
@@ -1062,6 +1376,7 @@ struct EventEngine::Impl {
     EvArgs args{};
     bool committed = false;
     int grid_blocks = 0;
+    int pool_grid = 0;          /* resident blocks of the pool transport        */
     size_t smem_bytes = 0;
     bool one = true;
     ~Impl() { for (Inst* i : inst) delete i; }
@@ -1079,6 +1394,9 @@ int EventEngine::configure(const nraps_opts& o, std::string& err) {
     if (o.events_per_pass) params.K = o.events_per_pass;
     if (o.passes) params.passes = o.passes;
     params.tail = o.tail_lanes;
+    params.pool = o.pool_slots;
+    if (params.pool && (params.pool < 64 || params.pool > POOL_MAX)) { err = "pool_slots must be in [64, 4096]"; return NRAPS_ERR_INVALID; }
+    if (params.pool) { params.K = NRAPS_ONE_PASS; params.passes = 0; params.tail = 0; params.block = POOL_THREADS; }
     if (params.K == NRAPS_ONE_PASS && o.passes == 0) params.passes = 0;  /* every particle to its end in one pass */
     if (params.tail > 32) { err = "tail_lanes must be at most 32"; return NRAPS_ERR_INVALID; }
     if (params.tail && params.passes == 0) { err = "tail_lanes needs a following pass (passes >= 1)"; return NRAPS_ERR_INVALID; }
@@ -1313,10 +1631,22 @@ int EventEngine::size_grid() {
         per_sm < 1)
         per_sm = 1;
     m.grid_blocks = sms * per_sm;
+    m.pool_grid = 0;
+    if (m.one && params.pool && m.rec == nullptr) {
+        const void* pf = m.exact ? (m.mode == NRAPS_MODE_BANK ? (const void*)ev_pool<true, true> : (const void*)ev_pool<true, false>)
+                                 : (m.mode == NRAPS_MODE_BANK ? (const void*)ev_pool<false, true> : (const void*)ev_pool<false, false>);
+        const size_t pdyn = pool_bytes(params.pool) + m.smem_bytes;
+        int pb = 0;
+        if (pdyn <= 227 * 1024) {
+            cudaFuncSetAttribute(pf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pdyn);
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pb, pf, POOL_THREADS, pdyn) != cudaSuccess) pb = 0;
+        }
+        m.pool_grid = sms * pb;     /* 0: the pool does not fit, ev_pass runs */
+    }
     return NRAPS_OK;
 }
 
-uint64_t EventEngine::launches_per_generation() const { return 1 + params.passes; }
+uint64_t EventEngine::launches_per_generation() const { return impl_->pool_grid ? 1 : 1 + params.passes; }
 
 int EventEngine::enqueue_generation(cudaStream_t s, bool with_finalize, cudaEvent_t t0, cudaEvent_t t1) {
     Impl& m = *impl_;
@@ -1331,6 +1661,18 @@ int EventEngine::enqueue_generation(cudaStream_t s, bool with_finalize, cudaEven
     if (rec) {
         if (bank) { if (m.exact) EV_LAUNCH(true, true, true, true); else EV_LAUNCH(true, false, true, true); }
         else { if (m.exact) EV_LAUNCH(true, true, false, true); else EV_LAUNCH(true, false, false, true); }
+    } else if (m.one && m.pool_grid) {
+        const size_t pdyn = pool_bytes(params.pool) + m.smem_bytes;
+        const unsigned pg = (unsigned)std::min<uint64_t>((m.n_total + params.pool - 1) / params.pool,
+                                                         (uint64_t)m.pool_grid);
+        if (bank) {
+            if (m.exact) ev_pool<true, true><<<pg ? pg : 1, POOL_THREADS, pdyn, s>>>(a, params.pool);
+            else ev_pool<false, true><<<pg ? pg : 1, POOL_THREADS, pdyn, s>>>(a, params.pool);
+        } else {
+            if (m.exact) ev_pool<true, false><<<pg ? pg : 1, POOL_THREADS, pdyn, s>>>(a, params.pool);
+            else ev_pool<false, false><<<pg ? pg : 1, POOL_THREADS, pdyn, s>>>(a, params.pool);
+        }
+        r = cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
     } else if (m.one) {
         if (bank) { if (m.exact) EV_LAUNCH(true, true, true, false); else EV_LAUNCH(true, false, true, false); }
         else { if (m.exact) EV_LAUNCH(true, true, false, false); else EV_LAUNCH(true, false, false, false); }

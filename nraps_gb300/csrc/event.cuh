@@ -44,6 +44,8 @@ struct EvParams {
     uint32_t K = 4;         /* real collisions per particle per queue pass     */
     uint32_t passes = 3;    /* queue passes before the drain pass; 0 = one
                                pass that runs every particle to its end      */
+    uint32_t pool = 0;      /* > 0: the pool transport with this many particle
+                               slots per block (one pass; single instance) */
     uint32_t tail = 0;      /* a warp of a non-final pass whose input is used
                                up and that holds fewer live particles than
                                this re-queues them and leaves, so the next

@@ -70,10 +70,14 @@ def test_event_reflective_bitexact(ctx_factory):
     assert gkq == wkq and np.all(grec["fate"] != abi.FATE_LEAKED)
 
 
+# pool transport: particles in shared memory, block-wide phases (one instance)
+POOL_SHAPES = [dict(pool_slots=64), dict(pool_slots=1024)]
+
+
 def test_event_results_independent_of_queue_shape(ctx_factory):
     p = small(hist=20000, gens=10, skip=3)
     ks = []
-    for shape in SHAPES:
+    for shape in SHAPES + POOL_SHAPES:
         r = ctx_factory(seed=7, mode=abi.MODE_BANK, precision=abi.PREC_FP32,
                         tracking=abi.TRACK_WOODCOCK, **shape).solve(p)
         ks.append(r.k64)
@@ -146,7 +150,33 @@ def test_autotuner_leaves_results_unchanged(ctx_factory):
     s.close()
     fixed = ctx_factory(events_per_pass=4, passes=3, block_size=256, **base).solve(p)
     assert np.array_equal(r.k64, fixed.k64)
-    assert len(t["tried_ms"]) == 10 and min(t["tried_ms"]) > 0
+    assert len(t["tried_ms"]) == 8 and min(t["tried_ms"]) > 0
     assert t["block"] in (128, 256) and t["events_per_pass"] >= 1
     # one-pass shapes run every particle to its end (no queue passes)
     assert t["passes"] >= 1 or t["events_per_pass"] == abi.ONE_PASS
+
+
+@pytest.mark.parametrize("mode", [abi.MODE_PHYSICS, abi.MODE_BANK])
+def test_pool_transport_exact_log_matches(ctx_factory, mode):
+    """The pool transport against the warp transport with the shared
+    software logarithm: every history identical, so k, tallies and bank
+    order (entropy) agree exactly, and the sessions report one transport
+    launch per generation."""
+    p = small(hist=7000, gens=8, skip=3)
+    base = dict(seed=77, mode=mode, precision=abi.PREC_FP32, tracking=abi.TRACK_WOODCOCK, exact_log=1)
+    warp = ctx_factory(block_size=128, events_per_pass=abi.ONE_PASS, passes=0, **base).solve(p)
+    for slots in (64, 512, 4096):
+        pool = ctx_factory(pool_slots=slots, **base).solve(p)
+        assert np.array_equal(pool.k64, warp.k64), slots
+        np.testing.assert_allclose(pool.flux_mean, warp.flux_mean, rtol=1e-12, atol=0)
+        np.testing.assert_allclose(pool.entropy, warp.entropy, rtol=0, atol=1e-12)
+        assert pool.stats.collisions == warp.stats.collisions
+        assert pool.stats.transport_launches == p.generations
+
+
+def test_pool_slots_validated(ctx_factory):
+    p = small(hist=1000, gens=3, skip=1)
+    for bad in (1, 5000):
+        with pytest.raises(api.NrapsError):
+            ctx_factory(seed=1, mode=abi.MODE_BANK, precision=abi.PREC_FP32, tracking=abi.TRACK_WOODCOCK,
+                        pool_slots=bad).solve(p)
