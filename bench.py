@@ -155,7 +155,8 @@ ARMS = {
 }
 
 
-def measure_device(prob, arm: str, steps: int, warmup: int, seed: int, device: int, shape=None, pool=0):
+def measure_device(prob, arm: str, steps: int, warmup: int, seed: int, device: int, shape=None, pool=0,
+                   extra=None):
     """Device-resident throughput: per-step CUDA events on the engine stream.
     shape = (block, events_per_pass, passes[, tail_lanes]) fixes the event launch shape
     (no autotuning); None lets the engine tune it over the warm-up."""
@@ -168,6 +169,8 @@ def measure_device(prob, arm: str, steps: int, warmup: int, seed: int, device: i
             kw.update(tail_lanes=shape[3])
     if pool:
         kw.update(pool_slots=pool)
+    if extra:
+        kw.update(extra)
     ctx = api.Context(seed=seed, device=device, **kw)
     s = ctx.session(prob)
     s.set_profile(True)
@@ -263,7 +266,12 @@ def measure_scale_stress(seed: int, device: int):
     d = measure_device(prob, "event", prob.generations - prob.skip, prob.skip, seed, device)
     per_launch_ms = d["transport_ms"] / max(1, d["transport_launches"])
     coll_per_launch = d["collisions"] / max(1, d["transport_launches"])
+    # the same run started from the deterministic diffusion fission source
+    dd = measure_device(prob, "event", prob.generations - prob.skip, prob.skip, seed, device,
+                        extra=dict(initial_source=1))
     return {"workload": "scale_stress", "cells": prob.n_cells, "regions": 10000, "groups": 8,
+            "diffusion_source": {"k_mean": dd["k_mean"], "sigma_k_pcm": dd["k_sigma"] * 1e5,
+                                 "histories_per_s": dd["histories"] / (dd["ms"] / 1000.0)},
             "histories_per_step": prob.histories, "steps": prob.generations - prob.skip,
             "histories_per_s": d["histories"] / (d["ms"] / 1000.0),
             "collisions_per_s": d["collisions"] / (d["ms"] / 1000.0),

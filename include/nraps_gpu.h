@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define NRAPS_ABI_VERSION 3u
+#define NRAPS_ABI_VERSION 4u
 
 /* ---- status codes ------------------------------------------------------- */
 #define NRAPS_OK              0
@@ -103,7 +103,11 @@ typedef struct nraps_opts {
                                     advanced in block-wide phases over
                                     compacted lists) with this many slots per
                                     block, 64..4096; 0 = tuned                */
-    uint32_t reserved[4];
+    uint32_t initial_source;     /* BANK: 0 = the reference's uniform fuel source
+                                    for generation 0; 1 = N sites drawn
+                                    (deterministically) from the fission source
+                                    of the deterministic diffusion solution  */
+    uint32_t reserved[3];
 } nraps_opts;
 
 /* Fill *o with the defaults (FP64 surface tracking, COMPAT, seed 1). */
@@ -452,6 +456,13 @@ typedef struct nraps_diffusion_info {
 } nraps_diffusion_info;
 int nraps_diffusion_solve(const nraps_problem* problem, uint64_t max_iterations, float* flux,
                           float* assembly_average, nraps_diffusion_info* info);
+/* An initial fission source from the diffusion solution: n_sites sites,
+   cell c chosen with probability proportional to sum_g nu sigf phi_g dx_c,
+   x stratified within the cell, group from the cell material's chi --
+   deterministic (stratified and low-discrepancy, no random numbers), sorted
+   by x.  out: caller-allocated n_sites.  info may be NULL. */
+int nraps_diffusion_source(const nraps_problem* problem, uint64_t n_sites, nraps_site* out,
+                           nraps_diffusion_info* info);
 
 /* Text of a status code. */
 const char* nraps_status_string(int status);

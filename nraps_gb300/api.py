@@ -110,6 +110,7 @@ def load(build_if_missing: bool = True):
     L.nraps_run_input.argtypes = [vp, C.c_char_p, C.c_char_p, P(abi.Stats)]
     L.nraps_diffusion_solve.argtypes = [P(abi.Problem), C.c_uint64, P(C.c_float), P(C.c_float),
                                         P(abi.DiffusionInfo)]
+    L.nraps_diffusion_source.argtypes = [P(abi.Problem), C.c_uint64, C.c_void_p, P(abi.DiffusionInfo)]
     L.nraps_status_string.argtypes = [C.c_int]
     L.nraps_status_string.restype = C.c_char_p
     _LIB = L
@@ -267,6 +268,15 @@ def diffusion_solve(prob: ProblemArrays, max_iterations: int = 0):
     return (flux.reshape(G, n), avg.reshape(G, n),
             dict(k=info.k, iterations=info.iterations, converged=bool(info.converged),
                  delta_flux=info.delta_flux, delta_k=info.delta_k))
+
+
+def diffusion_source(prob: ProblemArrays, n_sites: int) -> np.ndarray:
+    """n_sites initial fission sites from the diffusion solution (SITE_DTYPE)."""
+    L = load()
+    out = np.zeros(n_sites, abi.SITE_DTYPE)
+    pv = prob.view()
+    _check(L.nraps_diffusion_source(C.byref(pv), n_sites, out.ctypes.data_as(C.c_void_p), None))
+    return out
 
 
 def run_input(input_path: str = "./TestCaseC.txt", out_dir: str = ".", ctx: "Context | None" = None):

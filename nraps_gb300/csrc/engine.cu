@@ -59,6 +59,9 @@ int validate_problem(nraps_ctx* ctx, const nraps_problem* p, const nraps_opts& o
     if (o.tracking == NRAPS_TRACK_WOODCOCK && (o.mode == NRAPS_MODE_COMPAT || o.precision != NRAPS_PREC_FP32))
         return set_err(ctx, NRAPS_ERR_INVALID, "WOODCOCK tracking runs PHYSICS or BANK mode in FP32");
     if (o.entropy_bins != 0) return set_err(ctx, NRAPS_ERR_INVALID, "entropy_bins must be 0 (one bin per cell)");
+    if (o.initial_source > 1) return set_err(ctx, NRAPS_ERR_INVALID, "initial_source must be 0 (uniform fuel) or 1 (diffusion)");
+    if (o.initial_source && o.mode != NRAPS_MODE_BANK)
+        return set_err(ctx, NRAPS_ERR_INVALID, "initial_source = 1 needs BANK mode (a fission bank to start from)");
     if (v.histories == 0) return set_err(ctx, NRAPS_ERR_INVALID, "Histories is 0");
     if (v.histories + o.compat_threads >= (1ULL << 32)) return set_err(ctx, NRAPS_ERR_INVALID, "at most 2^32-1 histories per generation");
     if (v.generations == 0) return set_err(ctx, NRAPS_ERR_INVALID, "Generations is 0");
@@ -313,6 +316,16 @@ int create_session(nraps_ctx* ctx, const nraps_problem* p, bool with_records, nr
     std::memset(&g0, 0, sizeof g0);
     g0.k = (double)p->k_new;
     g0.inv_kf = (float)(1.0 / g0.k);
+    if (bank && s->o.initial_source == 1) {
+        /* generation 0 starts from the diffusion fission source instead of
+           the uniform fuel source: the kernels take a non-empty bank */
+        std::vector<nraps_site> sites(s->N);
+        int ds = nraps_diffusion_source(p, s->N, sites.data(), nullptr);
+        if (ds != NRAPS_OK) return set_err(ctx, ds, nraps_host::last_error());
+        CK(cudaStreamSynchronize(sm));
+        CK(cudaMemcpy(s->bank0.p, sites.data(), s->N * sizeof(nraps_site), cudaMemcpyHostToDevice));
+        g0.n_bank = s->N;
+    }
     CK(cudaMemcpyAsync(s->state.p, &g0, sizeof g0, cudaMemcpyHostToDevice, sm));
 
     s->ba.st = s->state.as<GenState>();

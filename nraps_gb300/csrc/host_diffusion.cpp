@@ -222,4 +222,59 @@ int nraps_diffusion_solve(const nraps_problem* p, uint64_t max_iterations, float
     return NRAPS_OK;
 }
 
+int nraps_diffusion_source(const nraps_problem* p, uint64_t n_sites, nraps_site* out, nraps_diffusion_info* info) {
+    if (!p || !out || n_sites == 0 || !p->mesh.mesh_left) {
+        nraps_host::set_error("nraps_diffusion_source: missing problem, output or sites");
+        return NRAPS_ERR_INVALID;
+    }
+    const uint64_t n = p->mesh.n_cells, G = p->variables.energygroups, M = p->variables.mattypes;
+    std::vector<float> flux(G * (n ? n : 1));
+    nraps_diffusion_info di{};
+    int s = nraps_diffusion_solve(p, 0, flux.data(), nullptr, &di);
+    if (s != NRAPS_OK) return s;
+    if (info) *info = di;
+    const nraps_xsdata& x = p->xsdata;
+    const uint8_t* mat = p->mesh.matid;
+    /* fission density per cell and its running sum */
+    std::vector<double> cdf(n + 1, 0.0);
+    for (uint64_t c = 0; c < n; ++c) {
+        double f = 0.0;
+        for (uint64_t g = 0; g < G; ++g)
+            f += (double)x.nut[mat[c] + M * g] * (double)x.sigf[mat[c] + M * g] * (double)flux[g * n + c];
+        cdf[c + 1] = cdf[c] + std::max(0.0, f) * (double)p->mesh.delta_x[c];
+    }
+    const double total = cdf[n];
+    if (!(total > 0.0)) {
+        nraps_host::set_error("nraps_diffusion_source: the diffusion solution has no fission source");
+        return NRAPS_ERR_INVALID;
+    }
+    /* chi CDFs as the transport kernels build them (f32 running sums) */
+    std::vector<float> chi(M * G);
+    for (uint64_t m = 0; m < M; ++m) {
+        float run = 0.0f;
+        for (uint64_t g = 0; g < G; ++g) { run += x.chit[m + M * g]; chi[m * G + g] = run; }
+    }
+    const double phi_golden = 0.6180339887498949;
+    uint64_t c = 0;
+    for (uint64_t i = 0; i < n_sites; ++i) {
+        const double t = ((double)i + 0.5) / (double)n_sites * total;
+        while (c + 1 < n && cdf[c + 1] <= t) ++c;
+        const double w = cdf[c + 1] - cdf[c];
+        double frac = w > 0.0 ? (t - cdf[c]) / w : 0.5;
+        frac = std::min(std::max(frac, 0.0), 1.0);
+        const float xs = (float)((double)p->mesh.mesh_left[c] + frac * (double)p->mesh.delta_x[c]);
+        /* group: a low-discrepancy uniform through the cell material's chi */
+        const double u = std::fmod(0.5 + (double)i * phi_golden, 1.0);
+        const float* cd = &chi[(uint64_t)mat[c] * G];
+        uint32_t g = 0;
+        for (uint64_t e = 0; e < G; ++e) g += (cd[e] < (float)u) ? 1u : 0u;
+        if (g > G - 1) g = (uint32_t)(G - 1);
+        out[i].x = xs;
+        out[i].cell = (uint32_t)c;
+        out[i].group = g;
+        out[i].pad = 0;
+    }
+    return NRAPS_OK;
+}
+
 } /* extern "C" */

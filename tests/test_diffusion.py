@@ -164,3 +164,33 @@ def test_dispatch_errors_without_gpu(lib, tmp_path):
     with pytest.raises(api.NrapsError) as e:
         api.run_input(str(tmp_path / "jac.txt"), str(tmp_path))
     assert e.value.status == abi.ERR_UNSUPPORTED
+
+
+def test_diffusion_source_sites(lib):
+    """The initial source: deterministic, sorted, each site inside its cell,
+    cell counts proportional to the diffusion fission density, groups from
+    the cell material's chi."""
+    inp = api.process_input(os.path.join(INPUTS, "TestCaseC.txt"))
+    mesh, fuel = api.mesh_gen(inp.matid, inp.variables, inp.delta_x)
+    prob = api.problem_from_input(inp, mesh, fuel)
+    n = 50000
+    a = api.diffusion_source(prob, n)
+    b = api.diffusion_source(prob, n)
+    assert np.array_equal(a, b)
+    assert np.all(np.diff(a["x"]) >= 0)
+    left, right = prob.mesh_left[a["cell"]], prob.mesh_right[a["cell"]]
+    assert np.all(a["x"] >= left - 1e-5) and np.all(a["x"] <= right + 1e-5)
+    flux, _, _ = api.diffusion_solve(prob)
+    G, M = prob.energygroups, prob.mattypes
+    m = prob.matid.astype(np.int64)
+    dens = sum(prob.nut[m + M * g].astype(np.float64) * prob.sigf[m + M * g] * flux[g] for g in range(G)) * prob.delta_x
+    want = n * dens / dens.sum()
+    got = np.bincount(a["cell"], minlength=prob.n_cells)
+    assert np.all(np.abs(got - want) <= 1.0 + 1e-9)
+    assert np.all(dens[a["cell"]] > 0)
+    # groups: chi of the site's material, within sampling resolution
+    for mat in np.unique(m[a["cell"]]):
+        sel = m[a["cell"]] == mat
+        chi = np.array([prob.chit[mat + M * g] for g in range(G)], np.float64)
+        frac = np.bincount(a["group"][sel], minlength=G) / sel.sum()
+        np.testing.assert_allclose(frac, chi / chi.sum(), atol=2e-3)

@@ -180,3 +180,23 @@ def test_pool_slots_validated(ctx_factory):
         with pytest.raises(api.NrapsError):
             ctx_factory(seed=1, mode=abi.MODE_BANK, precision=abi.PREC_FP32, tracking=abi.TRACK_WOODCOCK,
                         pool_slots=bad).solve(p)
+
+
+@pytest.mark.parametrize("tracking", [abi.TRACK_WOODCOCK, abi.TRACK_SURFACE])
+def test_diffusion_initial_source(ctx_factory, tracking):
+    """Generation 0 from the diffusion fission source: the first generations
+    differ from the uniform-fuel start, the two runs' entropies approach each
+    other (one converged source), and the diffusion start is reproducible."""
+    p = synth.single_large(2).with_(histories=20000, generations=30, skip=10)
+    prec = abi.PREC_FP32 if tracking == abi.TRACK_WOODCOCK else abi.PREC_FP64
+    base = dict(seed=5, mode=abi.MODE_BANK, precision=prec, tracking=tracking)
+    uni = ctx_factory(**base).solve(p)
+    dif = ctx_factory(initial_source=1, **base).solve(p)
+    dif2 = ctx_factory(initial_source=1, **base).solve(p)
+    assert np.array_equal(dif.k64, dif2.k64)
+    assert dif.entropy[0] != uni.entropy[0] and not np.array_equal(dif.k64[:3], uni.k64[:3])
+    # the two starts approach one converged source from either side
+    gap0 = abs(dif.entropy[0] - uni.entropy[0])
+    assert abs(dif.entropy[-5:].mean() - uni.entropy[-5:].mean()) < 0.6 * gap0
+    with pytest.raises(api.NrapsError):
+        ctx_factory(seed=5, mode=abi.MODE_PHYSICS, precision=prec, tracking=tracking, initial_source=1).solve(p)
