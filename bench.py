@@ -271,7 +271,10 @@ def measure_scale_stress(seed: int, device: int):
                         extra=dict(initial_source=1))
     return {"workload": "scale_stress", "cells": prob.n_cells, "regions": 10000, "groups": 8,
             "diffusion_source": {"k_mean": dd["k_mean"], "sigma_k_pcm": dd["k_sigma"] * 1e5,
-                                 "histories_per_s": dd["histories"] / (dd["ms"] / 1000.0)},
+                                 "histories_per_s": dd["histories"] / (dd["ms"] / 1000.0),
+                                 "collisions_per_s": dd["collisions"] / (dd["ms"] / 1000.0),
+                                 "collisions_per_history": dd["collisions"] / max(1, dd["histories"])},
+            "collisions_per_history": d["collisions"] / max(1, d["histories"]),
             "histories_per_step": prob.histories, "steps": prob.generations - prob.skip,
             "histories_per_s": d["histories"] / (d["ms"] / 1000.0),
             "collisions_per_s": d["collisions"] / (d["ms"] / 1000.0),
