@@ -3,9 +3,9 @@
  *
  * TEST INFRASTRUCTURE ONLY.  Only tests/, __graft_entry__.smoke() and
  * bench.py's CPU-baseline / reference arm may load this library; the product
- * (nraps_gb300) never does.  It is the checker for the CUDA path and the timed
- * stand-in for the reference CPU solver, which is Rust and cannot be built
- * here (no rustc/cargo, crates not vendored).
+ * (nraps_gb300) never does.  It is what the CUDA path is checked against and
+ * the timed stand-in for the reference CPU solver, which is Rust and cannot
+ * be built without rustc/cargo and its crates.
  *
  * Pinned by: the reference's own unit tests (src/mc_code.rs:392-556, restated
  * in tests/test_oracle_golden.py) and the pcg-c-basic known-answer stream,

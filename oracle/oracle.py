@@ -1,8 +1,8 @@
 """ctypes loader for the CPU oracle library (test infrastructure only).
 
 The oracle restates NRAPS's src/mc_code.rs and src/rand.rs on the CPU (see
-oracle/nraps_oracle.cpp for the line-by-line citations).  It is the checker
-for the CUDA path and the timed stand-in for the reference CPU solver.
+oracle/nraps_oracle.cpp for the line-by-line citations).  The CUDA path is
+checked against it, and it is the timed stand-in for the reference CPU solver.
 """
 from __future__ import annotations
 

@@ -1,4 +1,4 @@
-"""Generate the golden fixtures under tests/golden/ (run here, not on the GPU machine).
+"""Generate the golden fixtures under tests/golden/ (run where the reference sources are).
 
 Inputs: the reference's own input fixtures TestCaseA.txt, TestCaseB.txt and
 TestCaseC.txt (Apache-2.0, copied verbatim as test inputs) and its

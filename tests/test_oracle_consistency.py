@@ -1,4 +1,4 @@
-"""Self-consistency of the CPU oracle (the checker) on small problems."""
+"""Self-consistency of the CPU oracle on small problems."""
 import numpy as np
 
 from nraps_gb300 import abi, synth
