@@ -1658,9 +1658,14 @@ int EventEngine::enqueue_generation(cudaStream_t s, bool with_finalize, cudaEven
     int r;
 #define EV_LAUNCH(ONE, EXACT, BANK, REC) \
     r = launch_passes<ONE, EXACT, BANK, REC>(a, params, m.grid_blocks, ONE ? m.smem_bytes : 0, m.n_total, s)
-    if (rec) {
+    if (rec && m.one) {
         if (bank) { if (m.exact) EV_LAUNCH(true, true, true, true); else EV_LAUNCH(true, false, true, true); }
         else { if (m.exact) EV_LAUNCH(true, true, false, true); else EV_LAUNCH(true, false, false, true); }
+    } else if (rec) {
+        /* one instance whose tables do not fit shared memory: read them
+           from global memory, as batched launches do */
+        if (bank) { if (m.exact) EV_LAUNCH(false, true, true, true); else EV_LAUNCH(false, false, true, true); }
+        else { if (m.exact) EV_LAUNCH(false, true, false, true); else EV_LAUNCH(false, false, false, true); }
     } else if (m.one && m.pool_grid) {
         const size_t pdyn = pool_bytes(params.pool) + m.smem_bytes;
         const unsigned pg = (unsigned)std::min<uint64_t>((m.n_total + params.pool - 1) / params.pool,
