@@ -371,6 +371,9 @@ int  nraps_server_create(nraps_ctx* ctx, const nraps_server_opts* o, nraps_serve
 /* copies the problem; NRAPS_ERR_REJECTED if it can never fit the budget */
 int  nraps_server_submit(nraps_server* s, const nraps_problem* p, uint64_t seed, uint64_t* req_id);
 int  nraps_server_step(nraps_server* s, uint32_t* n_running, uint32_t* n_finished);
+/* Ids of requests retired since the last call (oldest first), at most cap;
+   *n receives how many were written. */
+int  nraps_server_finished(nraps_server* s, uint64_t* ids, uint32_t cap, uint32_t* n);
 /* NRAPS_ERR_PENDING while queued/running; fills out (may be NULL) when done */
 int  nraps_server_poll(nraps_server* s, uint64_t req_id, nraps_result* out, nraps_request_info* info);
 int  nraps_server_release(nraps_server* s, uint64_t req_id);

@@ -98,6 +98,7 @@ def load(build_if_missing: bool = True):
     L.nraps_server_step.argtypes = [vp, P(C.c_uint32), P(C.c_uint32)]
     L.nraps_server_poll.argtypes = [vp, C.c_uint64, P(abi.Result), P(abi.RequestInfo)]
     L.nraps_server_release.argtypes = [vp, C.c_uint64]
+    L.nraps_server_finished.argtypes = [vp, P(C.c_uint64), C.c_uint32, P(C.c_uint32)]
     L.nraps_server_stats.argtypes = [vp, P(C.c_uint64), P(C.c_uint64), P(C.c_uint32), P(C.c_uint32),
                                      P(C.c_double), P(C.c_uint64)]
     L.nraps_server_clock.argtypes = [vp]
@@ -552,6 +553,13 @@ class Server:
         r, f = C.c_uint32(), C.c_uint32()
         _check(self._L.nraps_server_step(self.h, C.byref(r), C.byref(f)), self.ctx.h)
         return r.value, f.value
+
+    def finished(self, cap: int = 4096) -> list:
+        """Ids of requests retired since the last call, oldest first."""
+        ids = (C.c_uint64 * cap)()
+        n = C.c_uint32()
+        _check(self._L.nraps_server_finished(self.h, ids, cap, C.byref(n)), self.ctx.h)
+        return [ids[i] for i in range(n.value)]
 
     def poll(self, rid: int, results: bool = True):
         """(status, info dict, ResultArrays or None); status ERR_PENDING while running."""

@@ -282,6 +282,7 @@ struct nraps_server {
     DevMem states;                       /* GenState per slot             */
     std::vector<uint32_t> free_slots;
     std::vector<GenState> host_states;
+    std::deque<uint64_t> finished;       /* retired, not yet reported by nraps_server_finished */
     uint64_t next_id = 1, bytes_in_use = 0, histories = 0, completed = 0;
     double busy_ms = 0.0;
     bool dirty = false;
@@ -404,7 +405,11 @@ int nraps_server_step(nraps_server* s, uint32_t* n_running, uint32_t* n_finished
     if (r < 0) { cudaEventDestroy(e0); cudaEventDestroy(e1); return set_err(ctx, NRAPS_ERR_CUDA, std::string("kernel launch failed: ") + cudaGetErrorString(cudaGetLastError())); }
     ctx->launches += (uint64_t)r;
     CK(cudaEventRecord(e1, sm));
-    CK(cudaMemcpyAsync(s->host_states.data(), s->states.p, s->host_states.size() * sizeof(GenState),
+    /* only the slots up to the highest one in use (slots are handed out
+       lowest first) */
+    uint32_t hi_slot = 0;
+    for (uint64_t id : s->running) hi_slot = std::max(hi_slot, s->reqs[id]->slot);
+    CK(cudaMemcpyAsync(s->host_states.data(), s->states.p, (size_t)(hi_slot + 1) * sizeof(GenState),
                        cudaMemcpyDeviceToHost, sm));
     CK(cudaStreamSynchronize(sm));
     float ms = 0.f;
@@ -438,6 +443,7 @@ int nraps_server_step(nraps_server* s, uint32_t* n_running, uint32_t* n_finished
             s->running.erase(s->running.begin() + i);
             s->dirty = true;
             s->completed++;
+            s->finished.push_back(q.id);
             ++fin;
         } else {
             ++i;
@@ -445,6 +451,18 @@ int nraps_server_step(nraps_server* s, uint32_t* n_running, uint32_t* n_finished
     }
     if (n_running) *n_running = (uint32_t)s->running.size();
     if (n_finished) *n_finished = fin;
+    return NRAPS_OK;
+}
+
+int nraps_server_finished(nraps_server* s, uint64_t* ids, uint32_t cap, uint32_t* n) {
+    if (!s || !n || (cap && !ids)) return NRAPS_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(s->mu);
+    uint32_t k = 0;
+    while (k < cap && !s->finished.empty()) {
+        ids[k++] = s->finished.front();
+        s->finished.pop_front();
+    }
+    *n = k;
     return NRAPS_OK;
 }
 

@@ -70,10 +70,8 @@ def run_poisson(ctx: api.Context, rate: float = 200.0, seconds: float = 20.0, se
             _, fin = srv.step()
             steps += 1
             if fin:
-                for rid in list(in_flight):
+                for rid in srv.finished():
                     s, info, _ = srv.poll(rid, results=False)
-                    if s == abi.ERR_PENDING:
-                        continue
                     idx, arr = submitted[rid]
                     lat.append(info["t_done"] - t0 - arr)
                     gens.append(info["generations_run"])

@@ -131,3 +131,23 @@ def test_server_budget(ctx_factory):
     st, info, _ = _run_until_done(srv, r2)
     assert st == abi.OK
     srv.close()
+
+
+def test_server_finished_ids(ctx_factory):
+    """nraps_server_finished reports each retired request once, in order."""
+    probs = instances(3, seed=9)
+    ctx = ctx_factory(seed=1, **WC)
+    srv = api.Server(ctx, sigma_k_target=1.0, min_active=2)
+    ids = [srv.submit(p, 10 + i) for i, p in enumerate(probs)]
+    seen = []
+    for _ in range(200):
+        srv.step()
+        seen += srv.finished()
+        if len(seen) == len(ids):
+            break
+    assert sorted(seen) == sorted(ids) and len(set(seen)) == len(seen)
+    assert srv.finished() == []
+    for rid in seen:
+        st, info, _ = srv.poll(rid, results=False)
+        assert st == abi.OK and info["generations_run"] >= 2
+    srv.close()
