@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define NRAPS_ABI_VERSION 4u
+#define NRAPS_ABI_VERSION 5u
 
 /* ---- status codes ------------------------------------------------------- */
 #define NRAPS_OK              0
@@ -107,7 +107,11 @@ typedef struct nraps_opts {
                                     for generation 0; 1 = N sites drawn
                                     (deterministically) from the fission source
                                     of the deterministic diffusion solution  */
-    uint32_t reserved[3];
+    uint32_t range_len;          /* WOODCOCK, one pass: > 0 = a ranged launch,
+                                    one block per range of this many histories
+                                    of one instance, that instance's tables in
+                                    shared memory; 0 = tuned / persistent     */
+    uint32_t reserved[2];
 } nraps_opts;
 
 /* Fill *o with the defaults (FP64 surface tracking, COMPAT, seed 1). */
@@ -256,8 +260,8 @@ int  nraps_session_timing(nraps_session* s, double* transport_ms, double* total_
    is kept; results do not depend on the shape.  tried_ms receives the
    transport time of each candidate tried (up to tried_cap). */
 int  nraps_session_tuning(nraps_session* s, uint32_t* block, uint32_t* events_per_pass,
-                          uint32_t* passes, uint32_t* tail_lanes, uint32_t* pool_slots, uint32_t* n_tried,
-                          float* tried_ms, uint32_t tried_cap);
+                          uint32_t* passes, uint32_t* tail_lanes, uint32_t* pool_slots, uint32_t* range_len,
+                          uint32_t* n_tried, float* tried_ms, uint32_t tried_cap);
 /* generations completed so far (enqueued work included after sync) */
 uint64_t nraps_session_generation(const nraps_session* s);
 void nraps_session_destroy(nraps_session* s);

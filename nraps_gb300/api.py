@@ -71,7 +71,7 @@ def load(build_if_missing: bool = True):
     L.nraps_session_timing.argtypes = [vp, P(C.c_double), P(C.c_double), P(C.c_uint64),
                                        P(C.c_uint64), P(C.c_uint64)]
     L.nraps_session_tuning.argtypes = [vp, P(C.c_uint32), P(C.c_uint32), P(C.c_uint32), P(C.c_uint32),
-                                       P(C.c_uint32), P(C.c_uint32), P(C.c_float), C.c_uint32]
+                                       P(C.c_uint32), P(C.c_uint32), P(C.c_uint32), P(C.c_float), C.c_uint32]
     L.nraps_trace_generation.argtypes = [vp, P(abi.Problem), C.c_uint64, C.c_double, vp, C.c_uint64,
                                          vp, C.c_uint64, P(C.c_double), vp, C.c_uint64,
                                          P(C.c_uint64), P(C.c_uint64)]
@@ -421,12 +421,12 @@ class Session:
                     collisions=coll.value, histories=hist.value)
 
     def tuning(self) -> dict:
-        b, k, pa, t, po, n = (C.c_uint32() for _ in range(6))
+        b, k, pa, t, po, rl, n = (C.c_uint32() for _ in range(7))
         ms = (C.c_float * 32)()
         _check(self._L.nraps_session_tuning(self.h, C.byref(b), C.byref(k), C.byref(pa), C.byref(t), C.byref(po),
-                                            C.byref(n), ms, 32), self.ctx.h)
+                                            C.byref(rl), C.byref(n), ms, 32), self.ctx.h)
         return dict(block=b.value, events_per_pass=k.value, passes=pa.value, tail_lanes=t.value,
-                    pool_slots=po.value, tried_ms=[ms[i] for i in range(min(n.value, 32))])
+                    pool_slots=po.value, range_len=rl.value, tried_ms=[ms[i] for i in range(min(n.value, 32))])
 
     @property
     def generation(self) -> int:

@@ -383,22 +383,24 @@ int create_session(nraps_ctx* ctx, const nraps_problem* p, bool with_records, nr
         if (est) return set_err(ctx, est, e2);
         /* tune block size, collisions per pass and pass count unless all given */
         if (!with_records && s->o.block_size == 0 && s->o.events_per_pass == 0 && s->o.passes == 0 &&
-            s->o.tail_lanes == 0 && s->o.pool_slots == 0) {
+            s->o.tail_lanes == 0 && s->o.pool_slots == 0 && s->o.range_len == 0) {
             /* {block, K, passes, tail, pool}; likeliest first: short
                inactive phases try only the head.  The pool transport is
                not a candidate: on the 1M-history slab it measured 60-75%
                slower than the warp transport (fewer instructions per flight
                did not make up for its block barriers and lower occupancy). */
             const uint32_t X = NRAPS_ONE_PASS;
-            const uint32_t cand[][5] = {{256, X, 0, 0, 0}, {128, X, 0, 0, 0}, {256, 16, 1, 0, 0},
-                                        {256, X, 1, 12, 0}, {256, 4, 1, 0, 0}, {128, X, 1, 12, 0},
-                                        {256, 8, 2, 0, 0}, {128, 16, 1, 0, 0}};
+            /* {block, K, passes, tail, pool, range} */
+            const uint32_t cand[][6] = {{256, X, 0, 0, 0, 0}, {128, X, 0, 0, 0, 1024}, {128, X, 0, 0, 0, 0},
+                                        {128, X, 0, 0, 0, 2048}, {256, X, 0, 0, 0, 2048}, {128, X, 0, 0, 0, 512},
+                                        {256, 16, 1, 0, 0, 0}, {256, X, 1, 12, 0, 0}, {256, 4, 1, 0, 0, 0},
+                                        {128, X, 0, 0, 0, 4096}};
             size_t n = sizeof(cand) / sizeof(cand[0]);
             size_t budget = (size_t)std::min<uint64_t>(s->v.skip, n);
             for (size_t i = 0; i < budget; ++i) {
                 EvParams pr;
                 pr.block = cand[i][0]; pr.K = cand[i][1]; pr.passes = cand[i][2]; pr.tail = cand[i][3];
-                pr.pool = cand[i][4];
+                pr.pool = cand[i][4]; pr.range = cand[i][5];
                 s->tune_cand.push_back(pr);
             }
             s->tuned = s->tune_cand.size() < 2;
@@ -644,8 +646,8 @@ int nraps_session_sync(nraps_session* s) {
 }
 
 int nraps_session_tuning(nraps_session* s, uint32_t* block, uint32_t* events_per_pass, uint32_t* passes,
-                         uint32_t* tail_lanes, uint32_t* pool_slots, uint32_t* n_tried, float* tried_ms,
-                         uint32_t tried_cap) {
+                         uint32_t* tail_lanes, uint32_t* pool_slots, uint32_t* range_len, uint32_t* n_tried,
+                         float* tried_ms, uint32_t tried_cap) {
     if (!s) return NRAPS_ERR_INVALID;
     if (!s->ev) return set_err(s->ctx, NRAPS_ERR_INVALID, "tuning applies to WOODCOCK sessions");
     if (block) *block = s->ev->params.block;
@@ -653,6 +655,7 @@ int nraps_session_tuning(nraps_session* s, uint32_t* block, uint32_t* events_per
     if (passes) *passes = s->ev->params.passes;
     if (tail_lanes) *tail_lanes = s->ev->params.tail;
     if (pool_slots) *pool_slots = s->ev->params.pool;
+    if (range_len) *range_len = s->ev->params.range;
     if (n_tried) *n_tried = (uint32_t)s->tune_ms.size();
     for (uint32_t i = 0; tried_ms && i < tried_cap && i < s->tune_ms.size(); ++i) tried_ms[i] = s->tune_ms[i];
     return NRAPS_OK;

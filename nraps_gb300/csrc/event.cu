@@ -62,6 +62,9 @@ struct NDiv {
     }
 };
 
+/* the largest per-instance table a ranged launch stages in shared memory */
+constexpr size_t RANGED_SMEM_MAX = 40 * 1024;
+
 constexpr uint32_t NLOG2N_TAB = 65536;
 constexpr double LOG2E = 1.4426950408889634;
 constexpr int SCATTER_ONE_THREADS = 512;
@@ -129,6 +132,12 @@ struct EvArgs {
     /* n*log2(n) for n < NLOG2N_TAB (FP64, filled once on the host with the
        shared logarithm): the entropy is log2(B) - sum_c n_c log2(n_c) / B */
     const double* nlog2n;
+    /* ranged launch of a batch (one-pass, every instance's tables fit shared
+       memory): block b takes range b of range_len histories of one instance,
+       stages that instance's tables and claims from a block-local counter.
+       range_begin[i] = ranges before instance i (n_inst+1 entries); 0 = off */
+    uint32_t range_len;
+    const uint32_t* range_begin;
 };
 
 /* table view: shared memory (single instance) or the instance's globals */
@@ -375,11 +384,37 @@ __global__ void __launch_bounds__(256, ONE ? 4 : 3) ev_pass(EvArgs a, int pass, 
         s_hot[threadIdx.x].inst = 0xFFFFFFFFu;
         s_pf[threadIdx.x].inst = 0xFFFFFFFFu;
     }
+    /* the instance this block runs (ONE: the only one, or, in a ranged batch
+       launch, the instance of the block's range) and the range it claims */
+    __shared__ unsigned long long s_claim;
+    __shared__ uint32_t s_inst0;
+    __shared__ unsigned long long s_rend;
+    if (ONE && threadIdx.x == 0) {
+        uint32_t i0 = 0;
+        unsigned long long rb = 0, re = a.n_total;
+        if (a.range_len) {
+            uint32_t lo = 0, hi = a.n_inst;
+            while (hi - lo > 1) {
+                const uint32_t mid = (lo + hi) >> 1;
+                if (a.range_begin[mid] <= blockIdx.x) lo = mid; else hi = mid;
+            }
+            i0 = lo;
+            const EvInst& I0 = a.inst[i0];
+            rb = I0.hist_begin + (unsigned long long)(blockIdx.x - a.range_begin[i0]) * a.range_len;
+            const unsigned long long iend = I0.hist_begin + I0.N;
+            re = rb + a.range_len < iend ? rb + a.range_len : iend;
+        }
+        s_inst0 = i0;
+        s_claim = rb;
+        s_rend = re;
+    }
+    if (ONE) __syncthreads();
+    const uint32_t inst0 = ONE ? s_inst0 : 0u;
     if (ONE) {
-        const EvInst& I = a.inst[0];
+        const EvInst& I = a.inst[inst0];
         unsigned char* tab = smem + (size_t)(blockDim.x >> 5) * sizeof(Stage);
         if (threadIdx.x == 0) {
-            load_hot(s_hot[0], I, 0, BANK);
+            load_hot(s_hot[0], I, inst0, BANK);
             if (SOURCE && BANK) {
                 const GenState* st = I.st;
                 s_src.bank = I.bank[st->gen & 1];
@@ -395,8 +430,9 @@ __global__ void __launch_bounds__(256, ONE ? 4 : 3) ev_pass(EvArgs a, int pass, 
     const unsigned FULL = 0xffffffffu;
     Stage& sg = s_stage[w];
     const int qin = (pass - 1) & 1, qout = pass & 1;
-    const uint64_t n_in = SOURCE ? a.n_total : a.qcount[pass - 1];
-    unsigned long long* claim = &a.claim[pass];
+    const bool ranged = ONE && SOURCE && a.range_len;
+    const uint64_t n_in = ranged ? s_rend : (SOURCE ? a.n_total : a.qcount[pass - 1]);
+    unsigned long long* claim = ranged ? &s_claim : &a.claim[pass];
     const uint32_t slab = (blockIdx.x * (blockDim.x >> 5) + w) % NSLAB;   /* every slab in use */
     uint64_t pool_next = 0, pool_end = 0;   /* warp-uniform claimed range     */
     uint64_t pf_base = 0;                   /* first index of the prefetch    */
@@ -408,7 +444,7 @@ __global__ void __launch_bounds__(256, ONE ? 4 : 3) ev_pass(EvArgs a, int pass, 
     Part p;
     uint32_t done = 0;
     uint64_t events = 0;
-    const EvInst* Ip = &a.inst[0];
+    const EvInst* Ip = &a.inst[inst0];
     TView tv = t;
     uint32_t tv_inst = 0xFFFFFFFFu;          /* batched: instance tv describes  */
     float inv_k = 0.0f;
@@ -437,7 +473,7 @@ __global__ void __launch_bounds__(256, ONE ? 4 : 3) ev_pass(EvArgs a, int pass, 
                         if (SOURCE) {
                             /* the whole birth here, two records per lane, so the
                                per-lane hand-out below is a copy */
-                            uint32_t inst = 0;
+                            uint32_t inst = inst0;
                             if (!ONE) {
                                 uint32_t lo = 0, hi = a.n_inst;
                                 while (hi - lo > 1) {
@@ -523,13 +559,13 @@ __global__ void __launch_bounds__(256, ONE ? 4 : 3) ev_pass(EvArgs a, int pass, 
                 const uint32_t pk = r4.w;
                 p.rng.state = sg.pf_rng[slot];
                 p.g = pk & 15u;
-                p.inst = ONE ? 0u : (pk >> 4) & 0xFFFu;
+                p.inst = ONE ? inst0 : (pk >> 4) & 0xFFFu;
                 p.seq = pk >> 16;
                 Hot& h = s_hot[ONE ? 0 : threadIdx.x];
                 if (!ONE && h.inst != p.inst) load_hot(h, a.inst[p.inst], p.inst, BANK);
                 p.local = (uint32_t)(p.id - h.hist_begin);
                 p.rng.inc = ((uint64_t)p.local << 1) | 1ULL;
-                Ip = &a.inst[ONE ? 0 : p.inst];
+                Ip = &a.inst[ONE ? inst0 : p.inst];
                 if (!ONE && p.inst != tv_inst) {
                     tv = global_view(*Ip);
                     tv_inst = p.inst;
@@ -711,7 +747,7 @@ __global__ void __launch_bounds__(256, ONE ? 4 : 3) ev_pass(EvArgs a, int pass, 
     if (!ONE && kq_part) atomicAdd(&a.inst[kq_inst].st->kq, kq_part);
     if (staged) flush_particles(a, sg, staged, pass, qout, lane);
     if (BANK && staged_sites) { if (!flush_sites(a, sg, staged_sites, slab, lane)) slab_full = true; }
-    if (slab_full && lane == 0) atomicOr(&a.inst[0].st->error, NR_ERR_CAPACITY);
+    if (slab_full && lane == 0) atomicOr(&a.inst[inst0].st->error, NR_ERR_CAPACITY);
     /* ---- counters: one atomic per warp ---------------------------------------- */
     unsigned long long kq = nrdev::warp_sum_u64(ONE ? acc.kq : 0ull);
     unsigned long long coll = nrdev::warp_sum_u64(acc.coll), virt = nrdev::warp_sum_u64(acc.virt);
@@ -719,7 +755,7 @@ __global__ void __launch_bounds__(256, ONE ? 4 : 3) ev_pass(EvArgs a, int pass, 
     unsigned long long cp = nrdev::warp_sum_u64(acc.capped);
     if (lane == 0) {
         GenState* s = a.stats;
-        if (ONE && kq) atomicAdd(&a.inst[0].st->kq, kq);
+        if (ONE && kq) atomicAdd(&a.inst[inst0].st->kq, kq);
         if (coll) atomicAdd(&s->collisions, coll);
         if (virt) atomicAdd(&s->virtual_collisions, virt);
         if (ab) atomicAdd(&s->absorbed, ab);
@@ -1377,6 +1413,12 @@ struct EventEngine::Impl {
     bool committed = false;
     int grid_blocks = 0;
     int pool_grid = 0;          /* resident blocks of the pool transport        */
+    /* ranged launch: every instance's tables fit shared memory */
+    bool ranged_fit = false;
+    uint32_t range_built = 0;   /* range length d_range_begin was built for */
+    uint32_t ranged_blocks = 0;
+    size_t ranged_smem = 0;
+    DBuf<uint32_t> d_range_begin;
     size_t smem_bytes = 0;
     bool one = true;
     ~Impl() { for (Inst* i : inst) delete i; }
@@ -1395,6 +1437,9 @@ int EventEngine::configure(const nraps_opts& o, std::string& err) {
     if (o.passes) params.passes = o.passes;
     params.tail = o.tail_lanes;
     params.pool = o.pool_slots;
+    params.range = o.range_len;
+    if (params.range && (params.range < 64 || params.range > (1u << 24))) { err = "range_len must be in [64, 2^24]"; return NRAPS_ERR_INVALID; }
+    if (params.range) { params.K = NRAPS_ONE_PASS; params.passes = 0; params.tail = 0; params.pool = 0; }
     if (params.pool && (params.pool < 64 || params.pool > POOL_MAX)) { err = "pool_slots must be in [64, 4096]"; return NRAPS_ERR_INVALID; }
     if (params.pool) { params.K = NRAPS_ONE_PASS; params.passes = 0; params.tail = 0; params.block = POOL_THREADS; }
     if (params.K == NRAPS_ONE_PASS && o.passes == 0) params.passes = 0;  /* every particle to its end in one pass */
@@ -1601,6 +1646,19 @@ int EventEngine::commit(cudaStream_t s, std::string& err) {
         if (sb <= 120 * 1024) { m.one = true; m.smem_bytes = sb; }
     }
     a.hist_smem = (m.one && bank && m.inst[0]->d.nc <= HIST_SMEM_MAX_CELLS) ? 1 : 0;
+    /* ranged launches: do every instance's tables fit shared memory? */
+    a.range_len = 0;
+    a.range_begin = nullptr;
+    {
+        size_t tmax = 0;
+        for (uint32_t i = 0; i < n; ++i) {
+            const EvInst& I = m.inst[i]->d;
+            tmax = std::max(tmax, smem_bytes_for(I.M, I.G, I.R, I.nbins));
+        }
+        m.ranged_fit = tmax <= RANGED_SMEM_MAX;
+        m.ranged_smem = (tmax + 15) / 16 * 16;
+        m.range_built = 0;
+    }
     if (!m.nlog2n.p) {
         std::vector<double> t(NLOG2N_TAB, 0.0);
         for (uint32_t i = 2; i < NLOG2N_TAB; ++i) t[i] = (double)i * nr_log((double)i) * LOG2E;
@@ -1617,6 +1675,18 @@ int EventEngine::commit(cudaStream_t s, std::string& err) {
 
 int EventEngine::size_grid() {
     Impl& m = *impl_;
+    if (params.range && m.ranged_fit && m.range_built != params.range && m.committed) {
+        /* range prefix for params.range histories per block */
+        const uint32_t n = (uint32_t)m.inst.size(), RL = params.range;
+        std::vector<uint32_t> rb(n + 1, 0);
+        for (uint32_t i = 0; i < n; ++i) rb[i + 1] = rb[i] + (uint32_t)((m.inst[i]->d.N + RL - 1) / RL);
+        if (m.d_range_begin.n < n + 1 && m.d_range_begin.alloc(std::max<size_t>(n + 1, 2 * m.d_range_begin.n)) != cudaSuccess)
+            return NRAPS_ERR_NOMEM;
+        if (cudaMemcpy(m.d_range_begin.p, rb.data(), (n + 1) * 4, cudaMemcpyHostToDevice) != cudaSuccess)
+            return NRAPS_ERR_CUDA;
+        m.ranged_blocks = rb[n];
+        m.range_built = RL;
+    }
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -1646,7 +1716,9 @@ int EventEngine::size_grid() {
     return NRAPS_OK;
 }
 
-uint64_t EventEngine::launches_per_generation() const { return impl_->pool_grid ? 1 : 1 + params.passes; }
+uint64_t EventEngine::launches_per_generation() const {
+    return (impl_->pool_grid || params.passes == 0) ? 1 : 1 + params.passes;
+}
 
 int EventEngine::enqueue_generation(cudaStream_t s, bool with_finalize, cudaEvent_t t0, cudaEvent_t t1) {
     Impl& m = *impl_;
@@ -1666,6 +1738,19 @@ int EventEngine::enqueue_generation(cudaStream_t s, bool with_finalize, cudaEven
            from global memory, as batched launches do */
         if (bank) { if (m.exact) EV_LAUNCH(false, true, true, true); else EV_LAUNCH(false, false, true, true); }
         else { if (m.exact) EV_LAUNCH(false, true, false, true); else EV_LAUNCH(false, false, false, true); }
+    } else if (params.range && params.passes == 0 && m.ranged_fit && m.range_built == params.range) {
+        EvArgs ar = a;
+        ar.range_len = params.range;
+        ar.range_begin = m.d_range_begin.p;
+        const size_t rs = stage_bytes(params.block) + m.ranged_smem;
+        if (bank) {
+            if (m.exact) { set_smem_attr<true, true, true, true, false>(rs); ev_pass<true, true, true, true, false><<<m.ranged_blocks, params.block, rs, s>>>(ar, 0, 0xFFFFFFFFu, 0u); }
+            else { set_smem_attr<true, true, false, true, false>(rs); ev_pass<true, true, false, true, false><<<m.ranged_blocks, params.block, rs, s>>>(ar, 0, 0xFFFFFFFFu, 0u); }
+        } else {
+            if (m.exact) { set_smem_attr<true, true, true, false, false>(rs); ev_pass<true, true, true, false, false><<<m.ranged_blocks, params.block, rs, s>>>(ar, 0, 0xFFFFFFFFu, 0u); }
+            else { set_smem_attr<true, true, false, false, false>(rs); ev_pass<true, true, false, false, false><<<m.ranged_blocks, params.block, rs, s>>>(ar, 0, 0xFFFFFFFFu, 0u); }
+        }
+        r = cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
     } else if (m.one && m.pool_grid) {
         const size_t pdyn = pool_bytes(params.pool) + m.smem_bytes;
         const unsigned pg = (unsigned)std::min<uint64_t>((m.n_total + params.pool - 1) / params.pool,

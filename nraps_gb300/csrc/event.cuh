@@ -46,6 +46,9 @@ struct EvParams {
                                pass that runs every particle to its end      */
     uint32_t pool = 0;      /* > 0: the pool transport with this many particle
                                slots per block (one pass; single instance) */
+    uint32_t range = 0;     /* > 0 (one pass): a ranged launch, one block per
+                               range of this many histories of one instance,
+                               that instance's tables in shared memory     */
     uint32_t tail = 0;      /* a warp of a non-final pass whose input is used
                                up and that holds fewer live particles than
                                this re-queues them and leaves, so the next
