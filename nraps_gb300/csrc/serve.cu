@@ -129,7 +129,8 @@ int nraps_batch_create(nraps_ctx* ctx, const nraps_problem* problems, uint32_t n
        9.4 ms for one persistent pass reading tables through L1 */
     if (ctx->opts.block_size == 0) b->ev.params.block = 128;
     if (ctx->opts.events_per_pass == 0 && ctx->opts.passes == 0) {
-        b->ev.params.K = NRAPS_ONE_PASS; b->ev.params.passes = 0; b->ev.params.range = 4096;
+        b->ev.params.K = NRAPS_ONE_PASS; b->ev.params.passes = 0;
+        b->ev.params.range = ctx->opts.range_len ? ctx->opts.range_len : 4096;
     } else if (ctx->opts.passes == 0 && b->ev.params.K != NRAPS_ONE_PASS) {
         b->ev.params.passes = 1;
     }
@@ -319,7 +320,8 @@ int nraps_server_create(nraps_ctx* ctx, const nraps_server_opts* opts, nraps_ser
     if ((st = s->ev.configure(ctx->opts, err))) return set_err(ctx, st, err);
     if (ctx->opts.block_size == 0) s->ev.params.block = 128;
     if (ctx->opts.events_per_pass == 0 && ctx->opts.passes == 0) {
-        s->ev.params.K = NRAPS_ONE_PASS; s->ev.params.passes = 0; s->ev.params.range = 4096;
+        s->ev.params.K = NRAPS_ONE_PASS; s->ev.params.passes = 0;
+        s->ev.params.range = ctx->opts.range_len ? ctx->opts.range_len : 4096;
     } else if (ctx->opts.passes == 0 && s->ev.params.K != NRAPS_ONE_PASS) {
         s->ev.params.passes = 1;
     }
