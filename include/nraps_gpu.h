@@ -107,10 +107,12 @@ typedef struct nraps_opts {
                                     for generation 0; 1 = N sites drawn
                                     (deterministically) from the fission source
                                     of the deterministic diffusion solution  */
-    uint32_t range_len;          /* WOODCOCK, one pass: > 0 = a ranged launch,
-                                    one block per range of this many histories
-                                    of one instance, that instance's tables in
-                                    shared memory; 0 = tuned / persistent     */
+    uint32_t range_len;          /* WOODCOCK, one pass: 64..32768 = a ranged
+                                    launch, one block per range of this many
+                                    histories of one instance, that instance's
+                                    tables in shared memory (BANK: the range
+                                    orders its own sites); 0 = tuned /
+                                    persistent                               */
     uint32_t reserved[2];
 } nraps_opts;
 

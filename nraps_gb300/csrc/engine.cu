@@ -88,8 +88,8 @@ cudaError_t InstBuffers::alloc(uint64_t G_, uint64_t nc_, uint64_t gens_, uint64
     A(fs_acc.alloc(nc * 8)); A(k64.alloc(gens * 8)); A(entropy.alloc(gens * 8));
     if (bank) {
         A(bank0.alloc(cap * sizeof(nraps_site))); A(bank1.alloc(cap * sizeof(nraps_site)));
-        A(hist.alloc(nc * EV_HIST_STRIDE * 4));
-        if (e == cudaSuccess) A(cudaMemsetAsync(hist.p, 0, nc * EV_HIST_STRIDE * 4, s));
+        A(hist.alloc(ev_hist_words(nc) * 4));
+        if (e == cudaSuccess) A(cudaMemsetAsync(hist.p, 0, ev_hist_words(nc) * 4, s));
     }
     if (st_ext) st = st_ext;
     else { A(own_state.alloc(sizeof(GenState))); st = own_state.as<GenState>(); }
@@ -297,7 +297,7 @@ int create_session(nraps_ctx* ctx, const nraps_problem* p, bool with_records, nr
             CK(cudaMemsetAsync(s->scount.p, 0, s->n_hist * 4, sm));
         }
         CK(s->bank0.alloc(s->cap * sizeof(nraps_site))); CK(s->bank1.alloc(s->cap * sizeof(nraps_site)));
-        uint64_t hist_words = s->nc * (woodcock ? EV_HIST_STRIDE : 1);
+        uint64_t hist_words = woodcock ? ev_hist_words(s->nc) : s->nc;
         CK(s->hist.alloc(hist_words * 4));
         CK(cudaMemsetAsync(s->hist.p, 0, hist_words * 4, sm));
     }

@@ -32,9 +32,6 @@ namespace {
 
 constexpr uint32_t NSLAB = 128;
 constexpr uint32_t MAX_PASSES = 16;
-/* one entropy counter per 128-byte line: the fuel cells' site counts then
-   spread over every L2 slice instead of a few dozen lines */
-constexpr uint32_t HIST_STRIDE = EV_HIST_STRIDE;
 /* cells of a shared-memory site histogram in the single-instance scatter */
 constexpr uint32_t HIST_SMEM_MAX_CELLS = 12288;
 /*
@@ -99,6 +96,7 @@ struct EvInst {
     nraps_site* bank[2];
     uint64_t bank_cap;
     uint32_t* hist;
+    uint32_t hist_shift;      /* site counter of cell c at hist[c << hist_shift] */
     uint64_t generations, skip, cell_begin;
     double conv_const;
 };
@@ -138,7 +136,32 @@ struct EvArgs {
        range_begin[i] = ranges before instance i (n_inst+1 entries); 0 = off */
     uint32_t range_len;
     const uint32_t* range_begin;
+    /* ranged bank (BANK mode, ranged launch): a block appends its range's
+       sites to chunks of RB_CHUNK records taken from a shared pool
+       (block-local fill counter, per-range chunk list), so the bank order is
+       later made per range from a block-local scan of the range's site
+       counts, with no scan over every history and no scatter across the
+       whole bank.  rb = 0: the site slabs of the other launches. */
+    int rb;
+    uint32_t rb_pool_chunks;
+    unsigned long long* rb_next;     /* chunks handed out this generation     */
+    uint32_t* rb_chunk;              /* ranges * RB_MAXC chunk ids              */
+    uint32_t* rb_fill;               /* ranges: sites the range appended        */
+    unsigned long long* rb_base;     /* ranges: first bank position in its instance */
+    unsigned long long* rb_total;    /* n_inst: sites of the generation         */
 };
+
+/* ranged bank geometry */
+constexpr uint32_t RB_CHUNK = 1024;          /* site records per chunk (16 KB)   */
+constexpr uint32_t RB_MAXC = 256;            /* chunks per range: 8 sites per
+                                                history of the longest range   */
+constexpr uint32_t RB_MAX_RANGE = 32768;     /* longest range (its scan is in
+                                                shared memory)                 */
+constexpr uint32_t RB_HIST_SMEM = 8192;      /* cells counted in shared memory   */
+constexpr uint32_t RB_THREADS = 256;
+constexpr uint32_t RB_UNSET = 0xFFFFFFFFu;   /* chunk not handed out yet         */
+constexpr uint32_t RB_FULL = 0xFFFFFFFEu;    /* the pool or the range is full    */
+constexpr uint32_t RB_SPIN_MAX = 1u << 20;   /* bound on waiting for a chunk id  */
 
 /* table view: shared memory (single instance) or the instance's globals */
 struct TView {
@@ -350,6 +373,43 @@ __device__ __forceinline__ bool flush_sites(const EvArgs& a, S& sg, uint32_t n, 
     return true;
 }
 
+/* flush the first n (<= 32) staged sites of a warp into its range's chunks
+   (warp-wide; ranged launches, block b = range b).  The warp whose
+   reservation holds the first slot of a chunk takes that chunk from the pool
+   and publishes its id in shared memory; a warp that reaches a chunk first
+   waits for the id (bounded).  Returns false (all lanes) when the range or
+   the pool is full or the wait ran out. */
+template <class S>
+__device__ __forceinline__ bool flush_range_sites(const EvArgs& a, S& sg, uint32_t n, uint32_t lane,
+                                                  uint32_t* s_fill, volatile uint32_t* s_chunk) {
+    uint32_t p0 = 0;
+    if (lane == 0) {
+        p0 = atomicAdd(s_fill, n);
+        /* n <= 32 < RB_CHUNK: at most one chunk starts in [p0, p0 + n) */
+        const uint32_t c = (p0 + RB_CHUNK - 1) / RB_CHUNK;
+        if (c * RB_CHUNK < p0 + n && c < RB_MAXC) {
+            const unsigned long long id = atomicAdd(a.rb_next, 1ULL);
+            const uint32_t v = id < a.rb_pool_chunks ? (uint32_t)id : RB_FULL;
+            a.rb_chunk[(uint64_t)blockIdx.x * RB_MAXC + c] = v;
+            s_chunk[c] = v;
+        }
+    }
+    p0 = __shfl_sync(0xffffffffu, p0, 0);
+    bool ok = true;
+    if (lane < n) {
+        const uint32_t pos = p0 + lane, c = pos / RB_CHUNK;
+        uint32_t id = RB_FULL;
+        if (c < RB_MAXC) id = s_chunk[c];
+        for (uint32_t spin = 0; id == RB_UNSET && spin < RB_SPIN_MAX; ++spin) {
+            __nanosleep(64);
+            id = s_chunk[c];
+        }
+        ok = id < RB_FULL;
+        if (ok) a.sites[(uint64_t)id * RB_CHUNK + (pos & (RB_CHUNK - 1))] = sg.site[lane];
+    }
+    return __all_sync(0xffffffffu, ok);
+}
+
 __device__ __forceinline__ void move_down(Stage& sg, uint32_t from, uint32_t n, uint32_t lane, bool sites) {
     /* entries [from, from+n) -> [0, n), n <= 32 */
     if (sites) {
@@ -371,8 +431,11 @@ __device__ __forceinline__ void move_down(Stage& sg, uint32_t from, uint32_t n, 
  * lanes, fly every live lane once per iteration, process real collisions,
  * stage fission sites and particles that completed K real collisions.
  */
-template <bool SOURCE, bool ONE, bool EXACT, bool BANK, bool REC>
+template <bool SOURCE, int ONE, bool EXACT, bool BANK, bool REC>
 __global__ void __launch_bounds__(256, ONE ? 4 : 3) ev_pass(EvArgs a, int pass, uint32_t K, uint32_t tail) {
+    /* ONE: 0 batched (instances mixed in a warp), 1 one instance, 2 ranged
+       (block b runs range b of one instance; tables of that instance) */
+    constexpr bool RANGED = ONE == 2;
     /* dynamic shared memory: one Stage per warp, then (ONE) the tables */
     extern __shared__ __align__(16) unsigned char smem[];
     Stage* s_stage = reinterpret_cast<Stage*>(smem);
@@ -389,10 +452,15 @@ __global__ void __launch_bounds__(256, ONE ? 4 : 3) ev_pass(EvArgs a, int pass, 
     __shared__ unsigned long long s_claim;
     __shared__ uint32_t s_inst0;
     __shared__ unsigned long long s_rend;
+    /* ranged bank: the range's fill and chunk ids */
+    __shared__ uint32_t s_rfill;
+    __shared__ uint32_t s_rchunk[RANGED ? RB_MAXC : 1];
+    if (RANGED)
+        for (uint32_t c = threadIdx.x; c < RB_MAXC; c += blockDim.x) s_rchunk[c] = RB_UNSET;
     if (ONE && threadIdx.x == 0) {
         uint32_t i0 = 0;
         unsigned long long rb = 0, re = a.n_total;
-        if (a.range_len) {
+        if (RANGED) {
             uint32_t lo = 0, hi = a.n_inst;
             while (hi - lo > 1) {
                 const uint32_t mid = (lo + hi) >> 1;
@@ -407,6 +475,7 @@ __global__ void __launch_bounds__(256, ONE ? 4 : 3) ev_pass(EvArgs a, int pass, 
         s_inst0 = i0;
         s_claim = rb;
         s_rend = re;
+        s_rfill = 0;
     }
     if (ONE) __syncthreads();
     const uint32_t inst0 = ONE ? s_inst0 : 0u;
@@ -430,7 +499,10 @@ __global__ void __launch_bounds__(256, ONE ? 4 : 3) ev_pass(EvArgs a, int pass, 
     const unsigned FULL = 0xffffffffu;
     Stage& sg = s_stage[w];
     const int qin = (pass - 1) & 1, qout = pass & 1;
-    const bool ranged = ONE && SOURCE && a.range_len;
+    const bool ranged = RANGED && SOURCE;
+    /* ranged BANK launches append sites to their range's chunks (a
+       compile-time choice: both flush paths in one kernel cost registers) */
+    constexpr bool rbk = BANK && RANGED && SOURCE;
     const uint64_t n_in = ranged ? s_rend : (SOURCE ? a.n_total : a.qcount[pass - 1]);
     unsigned long long* claim = ranged ? &s_claim : &a.claim[pass];
     const uint32_t slab = (blockIdx.x * (blockDim.x >> 5) + w) % NSLAB;   /* every slab in use */
@@ -690,7 +762,9 @@ __global__ void __launch_bounds__(256, ONE ? 4 : 3) ev_pass(EvArgs a, int pass, 
                 staged_sites += __popc(sm);
                 __syncwarp();
                 if (staged_sites >= 32) {
-                    if (!flush_sites(a, sg, 32, slab, lane)) slab_full = true;
+                    const bool fl = rbk ? flush_range_sites(a, sg, 32, lane, &s_rfill, s_rchunk)
+                                        : flush_sites(a, sg, 32, slab, lane);
+                    if (!fl) slab_full = true;
                     move_down(sg, 32, staged_sites - 32, lane, true);
                     staged_sites -= 32;
                 }
@@ -746,8 +820,16 @@ __global__ void __launch_bounds__(256, ONE ? 4 : 3) ev_pass(EvArgs a, int pass, 
     __syncwarp();
     if (!ONE && kq_part) atomicAdd(&a.inst[kq_inst].st->kq, kq_part);
     if (staged) flush_particles(a, sg, staged, pass, qout, lane);
-    if (BANK && staged_sites) { if (!flush_sites(a, sg, staged_sites, slab, lane)) slab_full = true; }
+    if (BANK && staged_sites) {
+        const bool fl = rbk ? flush_range_sites(a, sg, staged_sites, lane, &s_rfill, s_rchunk)
+                            : flush_sites(a, sg, staged_sites, slab, lane);
+        if (!fl) slab_full = true;
+    }
     if (slab_full && lane == 0) atomicOr(&a.inst[inst0].st->error, NR_ERR_CAPACITY);
+    if (rbk) {
+        __syncthreads();
+        if (threadIdx.x == 0) a.rb_fill[blockIdx.x] = s_rfill;
+    }
     /* ---- counters: one atomic per warp ---------------------------------------- */
     unsigned long long kq = nrdev::warp_sum_u64(ONE ? acc.kq : 0ull);
     unsigned long long coll = nrdev::warp_sum_u64(acc.coll), virt = nrdev::warp_sum_u64(acc.virt);
@@ -1081,45 +1163,104 @@ __device__ __forceinline__ uint32_t find_inst(const uint64_t* begin, uint32_t n,
 }
 
 /* ordered bank: site (parent, seq) -> offsets[parent] + seq - offsets[first
-   history of its instance]; blocks walk the filled part of one slab each */
-template <bool ONE>
+   history of its instance]; blocks walk the filled part of one slab each.
+   KIND: SCAT_ONE one instance (its descriptor once per thread); SCAT_TAB
+   every instance's destination (bank of the next generation, capacity,
+   counters, scan offset of its first history) staged once per block in
+   shared memory, so a site needs two independent loads (its parent's offset
+   and a shared-memory row) instead of a chain through the instance
+   descriptor and its GenState; SCAT_DIRECT the chain, for batches with more
+   instances than the table holds.  Each thread keeps SCAT_U sites in flight,
+   and lanes of a warp that add to the same site counter are merged into one
+   addition (match on the counter's address): the sites of one warp flush
+   are the children of neighbouring histories and often share a cell. */
+enum { SCAT_ONE = 0, SCAT_TAB = 1, SCAT_DIRECT = 2 };
+constexpr int SCAT_U = 4;
+constexpr uint32_t SCAT_TAB_MAX = 1536;   /* 29 B per instance: 43.5 KB */
+constexpr size_t SCAT_TAB_BYTES = 29;
+
+template <int KIND>
 __global__ void __launch_bounds__(256) ev_scatter(EvArgs a) {
+    extern __shared__ unsigned long long s_tab[];
     const uint32_t slab = blockIdx.x % NSLAB;
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint64_t per = gridDim.x / NSLAB;
+    uint4** t_out = reinterpret_cast<uint4**>(s_tab);
+    uint32_t** t_hist = reinterpret_cast<uint32_t**>(s_tab + a.n_inst);
+    uint64_t* t_cap = reinterpret_cast<uint64_t*>(s_tab + 2 * (size_t)a.n_inst);
+    uint32_t* t_base = reinterpret_cast<uint32_t*>(s_tab + 3 * (size_t)a.n_inst);
+    uint8_t* t_shift = reinterpret_cast<uint8_t*>(t_base + a.n_inst);
+    if (KIND == SCAT_TAB) {
+        for (uint32_t i = threadIdx.x; i < a.n_inst; i += blockDim.x) {
+            const EvInst& I = a.inst[i];
+            t_out[i] = reinterpret_cast<uint4*>(I.bank[(I.st->gen + 1) & 1]);
+            t_hist[i] = I.hist;
+            t_cap[i] = I.bank_cap;
+            t_base[i] = a.offsets[I.hist_begin];
+            t_shift[i] = (uint8_t)I.hist_shift;
+        }
+        __syncthreads();
+    }
     uint64_t filled = a.slab_count[slab];
     if (filled > a.slab_cap) filled = a.slab_cap;
     const uint4* src = a.sites + (uint64_t)slab * a.slab_cap;
-    /* single instance: its descriptor fields once per thread */
-    nraps_site* out0 = nullptr;
+    uint4* out0 = nullptr;
     uint64_t cap0 = 0;
     uint32_t* hist0 = nullptr;
-    if (ONE) {
+    uint32_t shift0 = 0;
+    if (KIND == SCAT_ONE) {
         const EvInst& I = a.inst[0];
-        out0 = I.bank[(I.st->gen + 1) & 1];
+        out0 = reinterpret_cast<uint4*>(I.bank[(I.st->gen + 1) & 1]);
         cap0 = I.bank_cap;
         hist0 = I.hist;
+        shift0 = I.hist_shift;
     }
-    for (uint64_t j = (uint64_t)(blockIdx.x / NSLAB) * blockDim.x + threadIdx.x; j < filled;
-         j += per * blockDim.x) {
-        uint4 v = src[j];
-        uint32_t inst = v.w >> 16;
-        /* a slab that overflowed keeps stale records: never follow them */
-        if (v.z >= a.n_total || inst >= a.n_inst) continue;
-        uint32_t cell = v.y & 0x07FFFFFFu;
-        const uint4 s = make_uint4(v.x, cell, v.y >> 27, 0u);   /* nraps_site, one 16-byte store */
-        if (ONE) {
-            uint64_t pos = (uint64_t)a.offsets[v.z] + (v.w & 0xFFFFu);
-            if (pos < cap0) {
-                reinterpret_cast<uint4*>(out0)[pos] = s;
-                nrdev::red_add_u32(&hist0[(uint64_t)cell * HIST_STRIDE], 1u);
+    /* warp-uniform chunks of SCAT_U x 32 sites: every lane runs every
+       iteration, so the match below always has the full warp */
+    const uint64_t wpb = blockDim.x >> 5;
+    const uint64_t step = per * wpb * (SCAT_U * 32);
+    for (uint64_t j0 = ((uint64_t)(blockIdx.x / NSLAB) * wpb + warp) * (SCAT_U * 32); j0 < filled; j0 += step) {
+        uint4 v[SCAT_U];
+        bool ok[SCAT_U];
+#pragma unroll
+        for (int u = 0; u < SCAT_U; ++u) {
+            const uint64_t j = j0 + (uint64_t)u * 32 + lane;
+            ok[u] = j < filled;
+            v[u] = ok[u] ? src[j] : make_uint4(0, 0, 0, 0);
+            /* a slab that overflowed keeps stale records: never follow them */
+            ok[u] = ok[u] && v[u].z < a.n_total && (v[u].w >> 16) < a.n_inst;
+        }
+        uint32_t off[SCAT_U];
+#pragma unroll
+        for (int u = 0; u < SCAT_U; ++u) off[u] = ok[u] ? a.offsets[v[u].z] : 0u;
+#pragma unroll
+        for (int u = 0; u < SCAT_U; ++u) {
+            const uint32_t inst = v[u].w >> 16;
+            uint4* out;
+            uint32_t* hist;
+            uint32_t shift;
+            uint64_t cap, pos = (uint64_t)off[u] + (v[u].w & 0xFFFFu);
+            if (KIND == SCAT_ONE) {
+                out = out0; hist = hist0; cap = cap0; shift = shift0;
+            } else if (KIND == SCAT_TAB) {
+                const uint32_t i = ok[u] ? inst : 0u;
+                out = t_out[i]; hist = t_hist[i]; cap = t_cap[i]; shift = t_shift[i];
+                pos -= t_base[i];
+            } else {
+                out = nullptr; hist = nullptr; cap = 0; shift = 0;
+                if (ok[u]) {
+                    const EvInst& I = a.inst[inst];
+                    out = reinterpret_cast<uint4*>(I.bank[(I.st->gen + 1) & 1]);
+                    hist = I.hist; cap = I.bank_cap; shift = I.hist_shift;
+                    pos -= a.offsets[I.hist_begin];
+                }
             }
-        } else {
-            const EvInst& I = a.inst[inst];
-            uint64_t pos = (uint64_t)a.offsets[v.z] + (v.w & 0xFFFFu) - a.offsets[I.hist_begin];
-            if (pos < I.bank_cap) {
-                reinterpret_cast<uint4*>(I.bank[(I.st->gen + 1) & 1])[pos] = s;
-                nrdev::red_add_u32(&I.hist[(uint64_t)cell * HIST_STRIDE], 1u);
-            }
+            const bool w = ok[u] && pos < cap;
+            const uint32_t cell = v[u].y & 0x07FFFFFFu;
+            if (w) out[pos] = make_uint4(v[u].x, cell, v[u].y >> 27, 0u);   /* nraps_site, one 16-byte store */
+            uint32_t* h = w ? hist + ((uint64_t)cell << shift) : nullptr;
+            const unsigned peers = __match_any_sync(0xFFFFFFFFu, (unsigned long long)h);
+            if (w && lane == (uint32_t)(__ffs(peers) - 1)) nrdev::red_add_u32(h, (uint32_t)__popc(peers));
         }
     }
 }
@@ -1175,16 +1316,176 @@ __global__ void __launch_bounds__(SCATTER_ONE_THREADS) ev_scatter_hist(EvArgs a)
         }
     }
     __syncthreads();
-    /* non-zero bins into the instance's strided counters: ~NSLAB additions
+    /* non-zero bins into the instance's counters: ~NSLAB additions
        per fuel cell instead of one per site */
     for (uint32_t c = threadIdx.x; c < nc; c += blockDim.x)
-        if (s_h[c]) nrdev::red_add_u32(&I.hist[(uint64_t)c * HIST_STRIDE], s_h[c]);
+        if (s_h[c]) nrdev::red_add_u32(&I.hist[(uint64_t)c << I.hist_shift], s_h[c]);
+}
+
+/* the instance of range r of a ranged launch (ranges of instance i are
+   [range_begin[i], range_begin[i+1])) */
+__device__ __forceinline__ uint32_t range_inst(const EvArgs& a, uint32_t r) {
+    uint32_t lo = 0, hi = a.n_inst;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (a.range_begin[mid] <= r) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+/*
+ * Ranged bank, step 1 (one block per instance): the first bank position of
+ * each of the instance's ranges -- the exclusive scan of the ranges' fills
+ * -- and the generation's site total.
+ */
+__global__ void __launch_bounds__(RB_THREADS) ev_rb_scan(EvArgs a) {
+    constexpr uint32_t NW = RB_THREADS / 32;
+    __shared__ unsigned long long s_w[NW];
+    __shared__ unsigned long long s_carry;
+    const uint32_t i = blockIdx.x, lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const uint32_t r0 = a.range_begin[i], r1 = a.range_begin[i + 1];
+    if (threadIdx.x == 0) s_carry = 0;
+    __syncthreads();
+    for (uint32_t b = r0; b < r1; b += RB_THREADS) {
+        const uint32_t r = b + threadIdx.x;
+        const unsigned long long f = r < r1 ? a.rb_fill[r] : 0ULL;
+        unsigned long long x = f;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= (uint32_t)o) x += y;
+        }
+        if (lane == 31) s_w[w] = x;
+        __syncthreads();
+        if (w == 0) {
+            unsigned long long y = lane < NW ? s_w[lane] : 0ULL;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const unsigned long long z = __shfl_up_sync(0xffffffffu, y, o);
+                if (lane >= (uint32_t)o) y += z;
+            }
+            if (lane < NW) s_w[lane] = y;
+        }
+        __syncthreads();
+        const unsigned long long carry = s_carry;
+        if (r < r1) a.rb_base[r] = carry + (w ? s_w[w - 1] : 0ULL) + x - f;
+        __syncthreads();
+        if (threadIdx.x == 0) s_carry = carry + s_w[NW - 1];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) a.rb_total[i] = s_carry;
+}
+
+/*
+ * Ranged bank, step 2 (one block per range): the range's per-history site
+ * counts are scanned in shared memory, and every site the range appended
+ * goes to base + (sites of the range's earlier histories) + seq -- the
+ * (parent, seq) order of the whole instance, written into a window of the
+ * bank that only this block touches.  Sites are counted per cell in shared
+ * memory (instances of at most RB_HIST_SMEM cells; the non-zero bins are
+ * added to the instance's counters at the end) or, for larger instances,
+ * straight into the counters, one addition per distinct counter of a warp.
+ */
+constexpr int RB_U = 4;
+__global__ void __launch_bounds__(RB_THREADS) ev_rb_scatter(EvArgs a) {
+    extern __shared__ uint32_t s_rb[];           /* loc[range_len], hist[...] */
+    constexpr uint32_t NW = RB_THREADS / 32;
+    __shared__ uint32_t s_ck[RB_MAXC];
+    __shared__ uint32_t s_w[NW];
+    const uint32_t r = blockIdx.x, lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const uint32_t i0 = range_inst(a, r);
+    const EvInst& I = a.inst[i0];
+    const uint64_t rb = I.hist_begin + (uint64_t)(r - a.range_begin[i0]) * a.range_len;
+    const uint64_t iend = I.hist_begin + I.N;
+    const uint32_t nh = (uint32_t)((rb + a.range_len < iend ? rb + a.range_len : iend) - rb);
+    const uint32_t nc = I.nc;
+    const bool hsm = nc <= RB_HIST_SMEM;
+    uint32_t* loc = s_rb;
+    uint32_t* hs = s_rb + a.range_len;
+    if (hsm)
+        for (uint32_t c = threadIdx.x; c < nc; c += RB_THREADS) hs[c] = 0;
+    for (uint32_t c = threadIdx.x; c < RB_MAXC; c += RB_THREADS) s_ck[c] = a.rb_chunk[(uint64_t)r * RB_MAXC + c];
+    /* exclusive scan of the range's site counts: each thread a contiguous
+       run of ipt histories, then the block's run totals */
+    const uint32_t ipt = (nh + RB_THREADS - 1) / RB_THREADS;
+    const uint32_t j0 = threadIdx.x * ipt, j1 = j0 + ipt < nh ? j0 + ipt : nh;
+    uint32_t sum = 0;
+    for (uint32_t j = j0; j < j1; ++j) sum += a.count[rb + j];
+    uint32_t x = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= (uint32_t)o) x += y;
+    }
+    if (lane == 31) s_w[w] = x;
+    __syncthreads();
+    if (w == 0) {
+        uint32_t y = lane < NW ? s_w[lane] : 0u;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t z = __shfl_up_sync(0xffffffffu, y, o);
+            if (lane >= (uint32_t)o) y += z;
+        }
+        if (lane < NW) s_w[lane] = y;
+    }
+    __syncthreads();
+    uint32_t run = (w ? s_w[w - 1] : 0u) + x - sum;
+    for (uint32_t j = j0; j < j1; ++j) {
+        const uint32_t c = a.count[rb + j];
+        loc[j] = run;
+        run += c;
+    }
+    __syncthreads();
+    uint4* out = reinterpret_cast<uint4*>(I.bank[(I.st->gen + 1) & 1]);
+    const uint64_t cap = I.bank_cap, base = a.rb_base[r];
+    uint32_t* gh = I.hist;
+    const uint32_t sh = I.hist_shift;
+    uint32_t fill = a.rb_fill[r];
+    if (fill > RB_MAXC * RB_CHUNK) fill = RB_MAXC * RB_CHUNK;
+    /* block-uniform trip count: the match below always has the full warp */
+    for (uint32_t q0 = 0; q0 < fill; q0 += RB_THREADS * RB_U) {
+        uint4 v[RB_U];
+        bool ok[RB_U];
+#pragma unroll
+        for (int u = 0; u < RB_U; ++u) {
+            const uint32_t q = q0 + (uint32_t)u * RB_THREADS + threadIdx.x;
+            const uint32_t id = q < fill ? s_ck[q / RB_CHUNK] : RB_FULL;
+            ok[u] = id < RB_FULL;
+            v[u] = ok[u] ? a.sites[(uint64_t)id * RB_CHUNK + q % RB_CHUNK] : make_uint4(0, 0, 0, 0);
+        }
+#pragma unroll
+        for (int u = 0; u < RB_U; ++u) {
+            /* slots of a range that ran out of room hold stale records */
+            const uint64_t parent = v[u].z;
+            const uint32_t cell = v[u].y & 0x07FFFFFFu;
+            bool w8 = ok[u] && parent >= rb && parent < rb + nh && cell < nc;
+            uint64_t pos = 0;
+            if (w8) {
+                pos = base + loc[parent - rb] + (v[u].w & 0xFFFFu);
+                w8 = pos < cap;
+            }
+            if (w8) out[pos] = make_uint4(v[u].x, cell, v[u].y >> 27, 0u);   /* nraps_site */
+            if (hsm) {
+                if (w8) atomicAdd(&hs[cell], 1u);
+            } else {
+                uint32_t* h = w8 ? gh + ((uint64_t)cell << sh) : nullptr;
+                const unsigned peers = __match_any_sync(0xffffffffu, (unsigned long long)h);
+                if (w8 && lane == (uint32_t)(__ffs(peers) - 1)) nrdev::red_add_u32(h, (uint32_t)__popc(peers));
+            }
+        }
+    }
+    if (hsm) {
+        __syncthreads();
+        for (uint32_t c = threadIdx.x; c < nc; c += RB_THREADS)
+            if (hs[c]) nrdev::red_add_u32(&gh[(uint64_t)c << sh], hs[c]);
+    }
 }
 
 /* block-wide: pass counters and slab fills back to zero for the next
    generation (called by the block that closes a generation) */
 __device__ __forceinline__ void reset_pass_counters(const EvArgs& a) {
     for (uint32_t p = threadIdx.x; p < 2 * (MAX_PASSES + 2); p += blockDim.x) a.qcount[p] = 0;
+    if (threadIdx.x == 0) *a.rb_next = 0;
     for (uint32_t q = threadIdx.x; q < NSLAB; q += blockDim.x) a.slab_count[q] = 0;
 }
 
@@ -1258,7 +1559,7 @@ __device__ void finish_instance(const EvArgs& a, uint32_t i, const double* h_giv
     const unsigned long long nactive = st->nactive, tot_sites = st->tot_sites, tot_hist = st->tot_histories;
     const unsigned int err0 = st->error;
     unsigned long long B = 0;
-    if (a.bank) B = a.offsets[I.hist_begin + I.N] - a.offsets[I.hist_begin];
+    if (a.bank) B = a.rb ? a.rb_total[i] : a.offsets[I.hist_begin + I.N] - a.offsets[I.hist_begin];
     unsigned long long c[5] = {0, 0, 0, 0, 0}, t[5] = {0, 0, 0, 0, 0};
     if (a.n_inst == 1) {
         c[0] = st->collisions; c[1] = st->virtual_collisions; c[2] = st->absorbed; c[3] = st->leaked;
@@ -1323,13 +1624,13 @@ __global__ void __launch_bounds__(FIN_THREADS) ev_finalize(EvArgs a) {
             uint32_t cnt = 0;
             uint64_t B = 0;
             if (a.bank) {
-                cnt = I.hist[c * HIST_STRIDE];
-                B = a.offsets[I.hist_begin + I.N] - a.offsets[I.hist_begin];
+                cnt = I.hist[c << I.hist_shift];
+                B = a.rb ? a.rb_total[inst] : a.offsets[I.hist_begin + I.N] - a.offsets[I.hist_begin];
             }
             if (gen < I.generations) {
                 fold_cell(I, c, gen, k);
                 if (a.bank) {
-                    I.hist[c * HIST_STRIDE] = 0;
+                    I.hist[c << I.hist_shift] = 0;
                     if (cnt && B) h = -nlog2n(a, cnt) / (double)B;
                 }
             }
@@ -1419,6 +1720,13 @@ struct EventEngine::Impl {
     uint32_t ranged_blocks = 0;
     size_t ranged_smem = 0;
     DBuf<uint32_t> d_range_begin;
+    /* ranged bank buffers (the site pool shares the slab buffer) */
+    bool rb_ok = false;             /* ranged launches use the ranged bank      */
+    uint32_t rb_pool_chunks = 0;
+    uint32_t rb_hist_cells = 0;     /* largest instance counted in shared memory */
+    uint64_t bank_sum = 0;
+    DBuf<uint32_t> rb_chunk, rb_fill;
+    DBuf<unsigned long long> rb_base, rb_total;
     size_t smem_bytes = 0;
     bool one = true;
     ~Impl() { for (Inst* i : inst) delete i; }
@@ -1438,7 +1746,7 @@ int EventEngine::configure(const nraps_opts& o, std::string& err) {
     params.tail = o.tail_lanes;
     params.pool = o.pool_slots;
     params.range = o.range_len;
-    if (params.range && (params.range < 64 || params.range > (1u << 24))) { err = "range_len must be in [64, 2^24]"; return NRAPS_ERR_INVALID; }
+    if (params.range && (params.range < 64 || params.range > RB_MAX_RANGE)) { err = "range_len must be in [64, 32768]"; return NRAPS_ERR_INVALID; }
     if (params.range) { params.K = NRAPS_ONE_PASS; params.passes = 0; params.tail = 0; params.pool = 0; }
     if (params.pool && (params.pool < 64 || params.pool > POOL_MAX)) { err = "pool_slots must be in [64, 4096]"; return NRAPS_ERR_INVALID; }
     if (params.pool) { params.K = NRAPS_ONE_PASS; params.passes = 0; params.tail = 0; params.block = POOL_THREADS; }
@@ -1504,6 +1812,7 @@ int EventEngine::add_instance(const nraps_problem& p, const EvBuffers& b, std::s
     d.flux_acc = b.flux_acc; d.fs_acc = b.fs_acc; d.flux_sum = b.flux_sum; d.flux_sq = b.flux_sq;
     d.k64 = b.k64; d.entropy = b.entropy;
     d.bank[0] = b.bank[0]; d.bank[1] = b.bank[1]; d.bank_cap = b.bank_cap; d.hist = b.hist;
+    d.hist_shift = ev_hist_shift(h.nc);
     d.generations = b.generations; d.skip = b.skip; d.conv_const = h.conv_const;
     in->b = b;
     impl_->inst.push_back(in);
@@ -1532,11 +1841,12 @@ GenState* EventEngine::batch_stats() const { return impl_->bstats.p; }
 
 uint64_t EventEngine::shared_bytes() const {
     const Impl* m = impl_;
-    return m->n_total * (24 * 2 + 8) + NSLAB * m->slab_cap * 16;
+    return m->n_total * (24 * 2 + 8) + m->sites.n * 16 + m->rb_chunk.n * 4 + m->rb_fill.n * 4 +
+           (m->rb_base.n + m->rb_total.n) * 8;
 }
 
 namespace {
-template <bool SOURCE, bool ONE, bool EXACT, bool BANK, bool REC>
+template <bool SOURCE, int ONE, bool EXACT, bool BANK, bool REC>
 void set_smem_attr(size_t smem) {
     static size_t granted = 48 * 1024;          /* the default dynamic limit         */
     if (smem > granted) {
@@ -1588,6 +1898,7 @@ int EventEngine::commit(cudaStream_t s, std::string& err) {
     std::vector<EvInst> d(n);
     uint64_t bank_sum = 0;
     for (uint32_t i = 0; i < n; ++i) { d[i] = m.inst[i]->d; bank_sum += m.inst[i]->b.bank_cap; }
+    m.bank_sum = bank_sum;
     cudaError_t e = cudaSuccess;
     auto A = [&](cudaError_t x) { if (e == cudaSuccess) e = x; };
     /* shared buffers grow geometrically, so a batch whose membership changes
@@ -1632,6 +1943,10 @@ int EventEngine::commit(cudaStream_t s, std::string& err) {
     a.blocks_done = m.qcount.p + 2 * (MAX_PASSES + 2);
     a.sites = m.sites.p;
     a.slab_count = m.slab_count.p; a.slab_cap = m.slab_cap;
+    a.rb = 0;
+    a.rb_next = m.qcount.p + 2 * (MAX_PASSES + 2) + 1;
+    a.rb_pool_chunks = 0;
+    a.rb_chunk = nullptr; a.rb_fill = nullptr; a.rb_base = nullptr; a.rb_total = nullptr;
     a.count = m.count.p; a.offsets = m.offsets.p;
     a.stats = (n == 1) ? m.inst[0]->d.st : m.bstats.p;
     a.max_events = m.max_events;
@@ -1686,6 +2001,31 @@ int EventEngine::size_grid() {
             return NRAPS_ERR_CUDA;
         m.ranged_blocks = rb[n];
         m.range_built = RL;
+        /* ranged bank: chunk lists, fills and bases per range, a pool with
+           room for every banked site plus one partial chunk per range */
+        m.rb_ok = false;
+        if (m.mode == NRAPS_MODE_BANK) {
+            const uint64_t R = m.ranged_blocks;
+            const uint64_t chunks = (m.bank_sum + RB_CHUNK - 1) / RB_CHUNK + R + 1;
+            if (chunks >= RB_FULL) return NRAPS_ERR_INVALID;
+            cudaError_t e = cudaSuccess;
+            auto A = [&](cudaError_t x) { if (e == cudaSuccess) e = x; };
+            if (m.rb_chunk.n < R * RB_MAXC) A(m.rb_chunk.alloc(R * RB_MAXC));
+            if (m.rb_fill.n < R) A(m.rb_fill.alloc(R));
+            if (m.rb_base.n < R) A(m.rb_base.alloc(R));
+            if (m.rb_total.n < n) A(m.rb_total.alloc(n));
+            if (m.sites.n < chunks * RB_CHUNK) {
+                A(m.sites.alloc(chunks * RB_CHUNK));
+                m.args.sites = m.sites.p;
+            }
+            if (e != cudaSuccess) return NRAPS_ERR_NOMEM;
+            uint32_t hc = 0;
+            for (uint32_t i = 0; i < n; ++i)
+                if (m.inst[i]->d.nc <= RB_HIST_SMEM) hc = std::max(hc, m.inst[i]->d.nc);
+            m.rb_hist_cells = hc;
+            m.rb_pool_chunks = (uint32_t)chunks;
+            m.rb_ok = true;
+        }
     }
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
@@ -1726,6 +2066,9 @@ int EventEngine::enqueue_generation(cudaStream_t s, bool with_finalize, cudaEven
     const EvArgs& a = m.args;
     bool bank = m.mode == NRAPS_MODE_BANK;
     bool rec = m.rec != nullptr;
+    /* arguments of the kernels after the transport (the ranged bank's
+       buffers when a ranged launch uses it) */
+    EvArgs ar = a;
     if (t0) cudaEventRecord(t0, s);
     int r;
 #define EV_LAUNCH(ONE, EXACT, BANK, REC) \
@@ -1738,17 +2081,23 @@ int EventEngine::enqueue_generation(cudaStream_t s, bool with_finalize, cudaEven
            from global memory, as batched launches do */
         if (bank) { if (m.exact) EV_LAUNCH(false, true, true, true); else EV_LAUNCH(false, false, true, true); }
         else { if (m.exact) EV_LAUNCH(false, true, false, true); else EV_LAUNCH(false, false, false, true); }
-    } else if (params.range && params.passes == 0 && m.ranged_fit && m.range_built == params.range) {
-        EvArgs ar = a;
+    } else if (params.range && params.passes == 0 && m.ranged_fit && m.range_built == params.range &&
+               (!bank || m.rb_ok)) {
         ar.range_len = params.range;
         ar.range_begin = m.d_range_begin.p;
+        if (bank) {
+            ar.rb = 1;
+            ar.rb_pool_chunks = m.rb_pool_chunks;
+            ar.rb_chunk = m.rb_chunk.p; ar.rb_fill = m.rb_fill.p;
+            ar.rb_base = m.rb_base.p; ar.rb_total = m.rb_total.p;
+        }
         const size_t rs = stage_bytes(params.block) + m.ranged_smem;
         if (bank) {
-            if (m.exact) { set_smem_attr<true, true, true, true, false>(rs); ev_pass<true, true, true, true, false><<<m.ranged_blocks, params.block, rs, s>>>(ar, 0, 0xFFFFFFFFu, 0u); }
-            else { set_smem_attr<true, true, false, true, false>(rs); ev_pass<true, true, false, true, false><<<m.ranged_blocks, params.block, rs, s>>>(ar, 0, 0xFFFFFFFFu, 0u); }
+            if (m.exact) { set_smem_attr<true, 2, true, true, false>(rs); ev_pass<true, 2, true, true, false><<<m.ranged_blocks, params.block, rs, s>>>(ar, 0, 0xFFFFFFFFu, 0u); }
+            else { set_smem_attr<true, 2, false, true, false>(rs); ev_pass<true, 2, false, true, false><<<m.ranged_blocks, params.block, rs, s>>>(ar, 0, 0xFFFFFFFFu, 0u); }
         } else {
-            if (m.exact) { set_smem_attr<true, true, true, false, false>(rs); ev_pass<true, true, true, false, false><<<m.ranged_blocks, params.block, rs, s>>>(ar, 0, 0xFFFFFFFFu, 0u); }
-            else { set_smem_attr<true, true, false, false, false>(rs); ev_pass<true, true, false, false, false><<<m.ranged_blocks, params.block, rs, s>>>(ar, 0, 0xFFFFFFFFu, 0u); }
+            if (m.exact) { set_smem_attr<true, 2, true, false, false>(rs); ev_pass<true, 2, true, false, false><<<m.ranged_blocks, params.block, rs, s>>>(ar, 0, 0xFFFFFFFFu, 0u); }
+            else { set_smem_attr<true, 2, false, false, false>(rs); ev_pass<true, 2, false, false, false><<<m.ranged_blocks, params.block, rs, s>>>(ar, 0, 0xFFFFFFFFu, 0u); }
         }
         r = cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
     } else if (m.one && m.pool_grid) {
@@ -1774,7 +2123,13 @@ int EventEngine::enqueue_generation(cudaStream_t s, bool with_finalize, cudaEven
     if (r < 0) return -1;
     if (t1) cudaEventRecord(t1, s);
     int n = r;
-    if (bank) {
+    if (bank && ar.rb) {
+        ev_rb_scan<<<a.n_inst, RB_THREADS, 0, s>>>(ar);
+        const size_t hb = ((size_t)ar.range_len + m.rb_hist_cells) * 4;
+        if (hb > 48 * 1024) cudaFuncSetAttribute(ev_rb_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hb);
+        ev_rb_scatter<<<m.ranged_blocks, RB_THREADS, hb, s>>>(ar);
+        n += 2;
+    } else if (bank) {
         int q = launch_exclusive_scan(m.count.p, m.n_total, m.block_sums.p, m.offsets.p, nullptr, s);
         if (q < 0) return -1;
         n += q;
@@ -1784,16 +2139,18 @@ int EventEngine::enqueue_generation(cudaStream_t s, bool with_finalize, cudaEven
                 cudaFuncSetAttribute(ev_scatter_hist, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hb);
             ev_scatter_hist<<<NSLAB * SCATTER_ONE_SPLIT, SCATTER_ONE_THREADS, hb, s>>>(a);
         } else if (m.one || rec) {
-            ev_scatter<true><<<NSLAB * 8, 256, 0, s>>>(a);
+            ev_scatter<SCAT_ONE><<<NSLAB * 8, 256, 0, s>>>(a);
+        } else if (a.n_inst <= SCAT_TAB_MAX) {
+            ev_scatter<SCAT_TAB><<<NSLAB * 8, 256, (size_t)a.n_inst * SCAT_TAB_BYTES, s>>>(a);
         } else {
-            ev_scatter<false><<<NSLAB * 8, 256, 0, s>>>(a);
+            ev_scatter<SCAT_DIRECT><<<NSLAB * 8, 256, 0, s>>>(a);
         }
         ++n;
     }
     if (with_finalize) {
         unsigned gb = (unsigned)std::min<uint64_t>((m.n_cells_total + FIN_THREADS - 1) / FIN_THREADS,
                                                    (uint64_t)m.grid_blocks * 4);
-        ev_finalize<<<gb ? gb : 1, FIN_THREADS, 0, s>>>(a);
+        ev_finalize<<<gb ? gb : 1, FIN_THREADS, 0, s>>>(ar);
         n += 1;
     }
     return cudaPeekAtLastError() == cudaSuccess ? n : -1;

@@ -32,12 +32,19 @@ struct EvBuffers {
     double *k64, *entropy;                 /* generations                    */
     nraps_site* bank[2];                   /* BANK mode ordered banks        */
     uint64_t bank_cap;
-    uint32_t* hist;                        /* nc * EV_HIST_STRIDE (BANK mode)  */
+    uint32_t* hist;                        /* ev_hist_words(nc) (BANK mode)  */
     uint64_t generations, skip;
     uint64_t seed;
 };
 
-#define EV_HIST_STRIDE 32  /* entropy counters are 128 B apart */
+/* Site counters of the entropy histogram.  An instance with few cells keeps
+   them 128 B apart (counter of cell c at word c << 5), so the additions to
+   its hot fuel cells spread over the L2 slices; a larger instance counts
+   densely, so its counters stay in L2 and neighbouring cells' additions
+   share sectors. */
+#define EV_HIST_SPREAD_MAX_CELLS 4096u
+__host__ __device__ inline uint32_t ev_hist_shift(uint64_t nc) { return nc <= EV_HIST_SPREAD_MAX_CELLS ? 5u : 0u; }
+__host__ __device__ inline uint64_t ev_hist_words(uint64_t nc) { return nc << ev_hist_shift(nc); }
 
 struct EvParams {
     uint32_t block = 256;   /* threads per block of the transport passes       */

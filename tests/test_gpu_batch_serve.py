@@ -45,7 +45,32 @@ def test_many_small_instances_equal_alone(ctx_factory):
         r = b.results(i)
         alone = ctx_factory(seed=seeds[i], **WC).solve(p)
         assert np.array_equal(r.k64, alone.k64), i
+        np.testing.assert_allclose(r.entropy, alone.entropy, rtol=1e-12, atol=1e-12)
         np.testing.assert_allclose(r.flux_mean, alone.flux_mean, rtol=1e-9, atol=0)
+    b.close()
+
+
+def test_more_instances_than_the_scatter_table(ctx_factory):
+    """1,600 instances: more than the bank scatter stages in shared memory
+    (1,536), so sites find their instance's bank through its descriptor;
+    sampled instances equal the same instance run alone, bank (through k of
+    the later generations) and site histogram (entropy) included."""
+    rng = np.random.default_rng(5)
+    probs = []
+    for _ in range(1600):
+        R = int(rng.integers(2, 6))
+        G = int(rng.integers(2, 4))
+        N = int(rng.integers(40, 200))
+        probs.append(synth.random_slab(rng, R, G, 0.5, 3.0, 4, N, 3, 1))
+    seeds = [9000 + i for i in range(len(probs))]
+    ctx = ctx_factory(seed=1, **WC)
+    b = api.Batch(ctx, probs, seeds=seeds)
+    b.run(probs[0].generations)
+    for i in range(0, len(probs), 97):
+        r = b.results(i)
+        alone = ctx_factory(seed=seeds[i], **WC).solve(probs[i])
+        assert np.array_equal(r.k64, alone.k64), i
+        np.testing.assert_allclose(r.entropy, alone.entropy, rtol=1e-12, atol=1e-12)
     b.close()
 
 

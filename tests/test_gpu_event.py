@@ -139,6 +139,18 @@ def test_event_bank_overflow_is_reported(ctx_factory):
     assert e.value.status == abi.ERR_CAPACITY
 
 
+def test_ranged_bank_overflow_is_reported(ctx_factory):
+    """Ranged launches append sites to chunks of a pool sized by the bank
+    capacity: a bank that cannot hold the generation's sites is reported
+    the same way."""
+    p = small(hist=5000, gens=4, skip=1)
+    ctx = ctx_factory(seed=3, mode=abi.MODE_BANK, precision=abi.PREC_FP32, tracking=abi.TRACK_WOODCOCK,
+                      bank_factor=0.01, range_len=1024)
+    with pytest.raises(api.NrapsError) as e:
+        ctx.solve(p)
+    assert e.value.status == abi.ERR_CAPACITY
+
+
 def test_autotuner_leaves_results_unchanged(ctx_factory):
     p = small(hist=20000, gens=16, skip=12)
     base = dict(seed=21, mode=abi.MODE_BANK, precision=abi.PREC_FP32, tracking=abi.TRACK_WOODCOCK)
@@ -206,13 +218,17 @@ def test_diffusion_initial_source(ctx_factory, tracking):
 def test_ranged_launch_exact_log_matches(ctx_factory, mode):
     """Ranged launches (one block per range of one instance, the tables in
     shared memory) against the persistent warp transport with the shared
-    logarithm: identical histories, so identical k, tallies and bank order."""
+    logarithm: identical histories, so identical k, tallies and bank order
+    (BANK: each range orders its own sites)."""
     p = small(hist=7000, gens=8, skip=3)
     base = dict(seed=78, mode=mode, precision=abi.PREC_FP32, tracking=abi.TRACK_WOODCOCK, exact_log=1)
     warp = ctx_factory(block_size=256, events_per_pass=abi.ONE_PASS, passes=0, **base).solve(p)
-    for rl, block in ((64, 128), (1000, 256), (8192, 128)):
+    for rl, block in ((64, 128), (1000, 256), (8192, 128), (32768, 256)):
         r = ctx_factory(range_len=rl, block_size=block, **base).solve(p)
         assert np.array_equal(r.k64, warp.k64), rl
         np.testing.assert_allclose(r.flux_mean, warp.flux_mean, rtol=1e-12, atol=0)
         np.testing.assert_allclose(r.entropy, warp.entropy, rtol=0, atol=1e-12)
         assert r.stats.collisions == warp.stats.collisions
+    with pytest.raises(api.NrapsError) as e:
+        ctx_factory(range_len=32769, **base).solve(p)
+    assert e.value.status == abi.ERR_INVALID
