@@ -357,6 +357,7 @@ def main():
                     help="block,events_per_pass,passes[,tail_lanes]: fixed event launch shape (profiling)")
     ap.add_argument("--pool", type=int, default=0, help="pool transport with this many slots per block (profiling)")
     ap.add_argument("--initial-source", type=int, default=0, help="1 = start from the diffusion fission source")
+    ap.add_argument("--range", type=int, default=0, help="ranged launches of this many histories (profiling)")
     ap.add_argument("--scale-stress", type=int, default=1, help="1 = also run the 10M-history, 200k-cell slab")
     args = ap.parse_args()
     if args.warmup < 3:
@@ -390,8 +391,13 @@ def main():
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
+    extra = {}
+    if args.initial_source:
+        extra["initial_source"] = args.initial_source
+    if args.range:
+        extra["range_len"] = args.range
     d = measure_device(prob, arm, args.steps, args.warmup, seed, local, shape=args.shape, pool=args.pool,
-                       extra=dict(initial_source=args.initial_source) if args.initial_source else None)
+                       extra=extra or None)
     clk = clocks.stop()
     ms = max_over_ranks(d["ms"], f"cuda:{local}")
     if world > 1:

@@ -258,9 +258,10 @@ int  nraps_session_timing(nraps_session* s, double* transport_ms, double* total_
                           uint64_t* histories);
 /* WOODCOCK sessions: the launch shape in use.  With block_size,
    events_per_pass and passes all 0 in the options, the first inactive
-   generations each try one candidate shape (synchronously) and the fastest
-   is kept; results do not depend on the shape.  tried_ms receives the
-   transport time of each candidate tried (up to tried_cap). */
+   generations each try one candidate shape (synchronously) and the one with
+   the least time per real collision is kept; results do not depend on the
+   shape.  tried_ms receives the whole-generation time of each candidate
+   tried (up to tried_cap). */
 int  nraps_session_tuning(nraps_session* s, uint32_t* block, uint32_t* events_per_pass,
                           uint32_t* passes, uint32_t* tail_lanes, uint32_t* pool_slots, uint32_t* range_len,
                           uint32_t* n_tried, float* tried_ms, uint32_t tried_cap);

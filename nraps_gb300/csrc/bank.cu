@@ -33,6 +33,8 @@ static_assert(SCAN_TILE == (1 << NR_SCAN_TILE_LOG2), "scan tile size");
 __global__ void __launch_bounds__(SCAN_THREADS) scan_tile_sums(const uint32_t* count, uint64_t n,
                                                                uint32_t* block_sums) {
     __shared__ uint32_t sw[33];
+    nrdev::pdl_trigger();
+    nrdev::pdl_wait();
     uint64_t base = (uint64_t)blockIdx.x * SCAN_TILE + (uint64_t)threadIdx.x * SCAN_ITEMS;
     uint32_t s = 0;
     for (int i = 0; i < SCAN_ITEMS; ++i) if (base + i < n) s += count[base + i];
@@ -44,6 +46,8 @@ __global__ void __launch_bounds__(SCAN_THREADS) scan_tile_sums(const uint32_t* c
 __global__ void __launch_bounds__(SCAN_THREADS) scan_top(uint32_t* block_sums, uint64_t nb,
                                                          unsigned long long* total, uint32_t* offsets_end) {
     __shared__ uint32_t sw[33];
+    nrdev::pdl_trigger();
+    nrdev::pdl_wait();
     uint32_t carry = 0;
     for (uint64_t b0 = 0; b0 < nb; b0 += SCAN_THREADS) {
         uint64_t i = b0 + threadIdx.x;
@@ -62,6 +66,8 @@ __global__ void __launch_bounds__(SCAN_THREADS) scan_top(uint32_t* block_sums, u
 __global__ void __launch_bounds__(SCAN_THREADS) scan_apply(const uint32_t* count, uint64_t n,
                                                            const uint32_t* block_sums, uint32_t* offsets) {
     __shared__ uint32_t sw[33];
+    nrdev::pdl_trigger();
+    nrdev::pdl_wait();
     uint64_t base = (uint64_t)blockIdx.x * SCAN_TILE + (uint64_t)threadIdx.x * SCAN_ITEMS;
     uint32_t v[SCAN_ITEMS];
     uint32_t s = 0;
@@ -85,6 +91,8 @@ __global__ void __launch_bounds__(SCAN_THREADS) scan_apply_carry(const uint32_t*
                                                                  const uint32_t* tile_sums, uint64_t nb,
                                                                  uint32_t* offsets, unsigned long long* total) {
     __shared__ uint32_t sw[33];
+    nrdev::pdl_trigger();
+    nrdev::pdl_wait();
     uint32_t c = 0;
     for (uint64_t i = threadIdx.x; i < blockIdx.x; i += SCAN_THREADS) c += tile_sums[i];
     uint32_t ex0;
@@ -230,17 +238,22 @@ __global__ void finalize_state(FinalizeArgs a) {
 }  // namespace
 
 int launch_exclusive_scan(const uint32_t* count, uint64_t n, uint32_t* block_sums, uint32_t* offsets,
-                          unsigned long long* total, cudaStream_t s) {
+                          unsigned long long* total, cudaStream_t s, bool pdl) {
     uint64_t nb = (n + SCAN_TILE - 1) / SCAN_TILE;
     if (nb == 0) return 0;
-    scan_tile_sums<<<(unsigned)nb, SCAN_THREADS, 0, s>>>(count, n, block_sums);
+    if (launch_k(pdl, scan_tile_sums, dim3((unsigned)nb), dim3(SCAN_THREADS), 0, s, count, n, block_sums) != cudaSuccess)
+        return -1;
     if (nb <= SCAN_CARRY_MAX_TILES) {
-        scan_apply_carry<<<(unsigned)nb, SCAN_THREADS, 0, s>>>(count, n, block_sums, nb, offsets, total);
-        return cudaPeekAtLastError() == cudaSuccess ? 2 : -1;
+        if (launch_k(pdl, scan_apply_carry, dim3((unsigned)nb), dim3(SCAN_THREADS), 0, s, count, n, block_sums, nb,
+                     offsets, total) != cudaSuccess)
+            return -1;
+        return 2;
     }
-    scan_top<<<1, SCAN_THREADS, 0, s>>>(block_sums, nb, total, offsets + n);
-    scan_apply<<<(unsigned)nb, SCAN_THREADS, 0, s>>>(count, n, block_sums, offsets);
-    return cudaPeekAtLastError() == cudaSuccess ? 3 : -1;
+    if (launch_k(pdl, scan_top, dim3(1), dim3(SCAN_THREADS), 0, s, block_sums, nb, total, offsets + n) != cudaSuccess ||
+        launch_k(pdl, scan_apply, dim3((unsigned)nb), dim3(SCAN_THREADS), 0, s, count, n, block_sums, offsets) !=
+            cudaSuccess)
+        return -1;
+    return 3;
 }
 
 int launch_bank_order(const BankArgs& a, cudaStream_t s) {

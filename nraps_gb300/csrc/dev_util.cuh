@@ -5,6 +5,17 @@
 
 namespace nrdev {
 
+/* Programmatic dependent launch (sm_90+).  A kernel launched with
+   programmatic stream serialization may start while the kernel before it
+   in the stream is still finishing; pdl_wait() blocks until that kernel
+   has completed and its memory is visible, so everything a kernel reads or
+   writes that the one before it produces or reads comes after it (reading
+   tables no kernel writes may come before).  A kernel launched without the
+   attribute returns from it at once.  pdl_trigger() lets the next kernel
+   launch as soon as every block of this one has started. */
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 __device__ __forceinline__ uint32_t warp_incl_scan(uint32_t v) {
     int lane = threadIdx.x & 31;
     for (int o = 1; o < 32; o <<= 1) {

@@ -223,7 +223,9 @@ struct nraps_session {
     uint64_t transport_launches = 0;
     /* autotuning of the event engine over the inactive generations */
     std::vector<EvParams> tune_cand;
-    std::vector<float> tune_ms;
+    std::vector<float> tune_ms;          /* whole generation per candidate        */
+    std::vector<double> tune_score;      /* ms per real collision                 */
+    unsigned long long tune_coll = 0;    /* collisions before the next candidate  */
     size_t tune_next = 0;
     bool tuned = false;
     ~nraps_session() {
@@ -560,21 +562,33 @@ int nraps_session_run(nraps_session* s, uint64_t n) {
             EvParams& pr = s->tune_cand[s->tune_next];
             s->ev->params = pr;
             s->ev->size_grid();
-            cudaEvent_t e0, e1;
-            CK(cudaEventCreate(&e0)); CK(cudaEventCreate(&e1));
-            int r = s->ev->enqueue_generation(sm, true, e0, e1);
+            /* a candidate is scored by its whole generation (transport, bank
+               ordering, finalize) per real collision: the source still moves
+               during the inactive generations, so histories get longer or
+               shorter from one candidate to the next */
+            cudaEvent_t e[4];
+            for (int j = 0; j < 4; ++j) CK(cudaEventCreate(&e[j]));
+            CK(cudaEventRecord(e[0], sm));
+            int r = s->ev->enqueue_generation(sm, true, e[1], e[2]);
             if (r < 0) return set_err(ctx, NRAPS_ERR_CUDA, std::string("kernel launch failed: ") + cudaGetErrorString(cudaGetLastError()));
+            CK(cudaEventRecord(e[3], sm));
             ctx->launches += (uint64_t)r;
             s->transport_launches += s->ev->launches_per_generation();
-            CK(cudaEventSynchronize(e1));
-            float ms = 0.f;
-            CK(cudaEventElapsedTime(&ms, e0, e1));
-            cudaEventDestroy(e0); cudaEventDestroy(e1);
+            CK(cudaEventSynchronize(e[3]));
+            float ms = 0.f, tms = 0.f;
+            CK(cudaEventElapsedTime(&ms, e[0], e[3]));
+            CK(cudaEventElapsedTime(&tms, e[1], e[2]));
+            for (int j = 0; j < 4; ++j) cudaEventDestroy(e[j]);
+            GenState g;
+            CK(cudaMemcpy(&g, s->state.p, sizeof g, cudaMemcpyDeviceToHost));
+            const unsigned long long coll = g.tot_collisions - s->tune_coll;
+            s->tune_coll = g.tot_collisions;
             s->tune_ms.push_back(ms);
-            s->transport_ms += ms;
+            s->tune_score.push_back(coll ? (double)ms / (double)coll : (double)ms);
+            s->transport_ms += tms;
             if (++s->tune_next == s->tune_cand.size()) {
                 size_t best = 0;
-                for (size_t j = 1; j < s->tune_ms.size(); ++j) if (s->tune_ms[j] < s->tune_ms[best]) best = j;
+                for (size_t j = 1; j < s->tune_score.size(); ++j) if (s->tune_score[j] < s->tune_score[best]) best = j;
                 s->ev->params = s->tune_cand[best];
                 s->ev->size_grid();
                 s->tuned = true;

@@ -113,13 +113,32 @@ struct FinalizeArgs {
     uint64_t bank_cap;
 };
 
+/* Launch k<<<g, b, smem, s>>>(args...), with programmatic stream
+   serialization when pdl (the kernel must call nrdev::pdl_wait() before it
+   touches what the previous kernel in the stream produces or reads). */
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_k(bool pdl, void (*k)(KArgs...), dim3 g, dim3 b, size_t smem, cudaStream_t s,
+                            Args&&... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = g;
+    cfg.blockDim = b;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = pdl ? at : nullptr;
+    cfg.numAttrs = pdl ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, k, static_cast<KArgs>(args)...);
+}
+
 /* launchers (each returns the number of kernels it launched, <0 on error) */
 template <class T>
 int launch_plain(const PlainArgs<T>& a, int mode, int block, cudaStream_t s);
 int launch_bank_order(const BankArgs& a, cudaStream_t s);
 /* offsets[i] = sum(count[0..i)), offsets[n] = total (offsets has n+1 slots) */
 int launch_exclusive_scan(const uint32_t* count, uint64_t n, uint32_t* block_sums, uint32_t* offsets,
-                          unsigned long long* total, cudaStream_t s);
+                          unsigned long long* total, cudaStream_t s, bool pdl = false);
 /* the scan works on tiles of 2^NR_SCAN_TILE_LOG2 counts; up to
    NR_SCAN_CARRY_MAX_TILES tiles it takes two launches, beyond that three */
 constexpr int NR_SCAN_TILE_LOG2 = 12;

@@ -21,6 +21,7 @@
  * batched launches read each particle's instance tables through L1.
  */
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 
 #include "dev_util.cuh"
@@ -431,11 +432,21 @@ __device__ __forceinline__ void move_down(Stage& sg, uint32_t from, uint32_t n, 
  * lanes, fly every live lane once per iteration, process real collisions,
  * stage fission sites and particles that completed K real collisions.
  */
+/* registers: 64 where the tables are in shared memory (one instance,
+   ranged); 80 where table pointers are global (batched, ranged over large
+   tables) */
 template <bool SOURCE, int ONE, bool EXACT, bool BANK, bool REC>
-__global__ void __launch_bounds__(256, ONE ? 4 : 3) ev_pass(EvArgs a, int pass, uint32_t K, uint32_t tail) {
+__global__ void __launch_bounds__(256, (ONE == 1 || ONE == 2) ? 4 : 3) ev_pass(EvArgs a, int pass, uint32_t K, uint32_t tail) {
     /* ONE: 0 batched (instances mixed in a warp), 1 one instance, 2 ranged
-       (block b runs range b of one instance; tables of that instance) */
-    constexpr bool RANGED = ONE == 2;
+       (block b runs range b of one instance, that instance's tables staged
+       in shared memory), 3 ranged with the tables read from global memory
+       (instances whose tables do not fit) */
+    constexpr bool RANGED = ONE >= 2;
+    constexpr bool SMEM_TAB = ONE == 1 || ONE == 2;
+    nrdev::pdl_trigger();
+    /* batched: every read below may depend on the previous kernel; one
+       instance: its tables are staged (and the range found) before the wait */
+    if (!ONE) nrdev::pdl_wait();
     /* dynamic shared memory: one Stage per warp, then (ONE) the tables */
     extern __shared__ __align__(16) unsigned char smem[];
     Stage* s_stage = reinterpret_cast<Stage*>(smem);
@@ -482,6 +493,9 @@ __global__ void __launch_bounds__(256, ONE ? 4 : 3) ev_pass(EvArgs a, int pass, 
     if (ONE) {
         const EvInst& I = a.inst[inst0];
         unsigned char* tab = smem + (size_t)(blockDim.x >> 5) * sizeof(Stage);
+        if (SMEM_TAB) stage_tables(I, tab, t);
+        else t = global_view(I);
+        nrdev::pdl_wait();
         if (threadIdx.x == 0) {
             load_hot(s_hot[0], I, inst0, BANK);
             if (SOURCE && BANK) {
@@ -491,7 +505,6 @@ __global__ void __launch_bounds__(256, ONE ? 4 : 3) ev_pass(EvArgs a, int pass, 
                 s_src.ndiv = I.ndiv;
             }
         }
-        stage_tables(I, tab, t);
         __syncthreads();
     }
     const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -880,6 +893,8 @@ __host__ __device__ __forceinline__ size_t pool_bytes(uint32_t P) {
 template <bool EXACT, bool BANK>
 __global__ void __launch_bounds__(POOL_THREADS, 2) ev_pool(EvArgs a, uint32_t P) {
     extern __shared__ __align__(16) unsigned char smem[];
+    nrdev::pdl_trigger();
+    nrdev::pdl_wait();
     __shared__ Hot s_h1;
     __shared__ SrcBank s_src;
     __shared__ uint32_t s_n[8];             /* live, next live, real, free, births, exhausted */
@@ -1182,6 +1197,8 @@ constexpr size_t SCAT_TAB_BYTES = 29;
 template <int KIND>
 __global__ void __launch_bounds__(256) ev_scatter(EvArgs a) {
     extern __shared__ unsigned long long s_tab[];
+    nrdev::pdl_trigger();
+    nrdev::pdl_wait();
     const uint32_t slab = blockIdx.x % NSLAB;
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint64_t per = gridDim.x / NSLAB;
@@ -1273,6 +1290,8 @@ __global__ void __launch_bounds__(256) ev_scatter(EvArgs a) {
    (site -> parent offset) in flight. */
 __global__ void __launch_bounds__(SCATTER_ONE_THREADS) ev_scatter_hist(EvArgs a) {
     extern __shared__ uint32_t s_h[];
+    nrdev::pdl_trigger();
+    nrdev::pdl_wait();
     const uint32_t b = blockIdx.x;
     const EvInst& I = a.inst[0];
     const uint32_t nc = I.nc;
@@ -1342,6 +1361,8 @@ __global__ void __launch_bounds__(RB_THREADS) ev_rb_scan(EvArgs a) {
     constexpr uint32_t NW = RB_THREADS / 32;
     __shared__ unsigned long long s_w[NW];
     __shared__ unsigned long long s_carry;
+    nrdev::pdl_trigger();
+    nrdev::pdl_wait();
     const uint32_t i = blockIdx.x, lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const uint32_t r0 = a.range_begin[i], r1 = a.range_begin[i + 1];
     if (threadIdx.x == 0) s_carry = 0;
@@ -1392,6 +1413,8 @@ __global__ void __launch_bounds__(RB_THREADS) ev_rb_scatter(EvArgs a) {
     constexpr uint32_t NW = RB_THREADS / 32;
     __shared__ uint32_t s_ck[RB_MAXC];
     __shared__ uint32_t s_w[NW];
+    nrdev::pdl_trigger();
+    nrdev::pdl_wait();
     const uint32_t r = blockIdx.x, lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const uint32_t i0 = range_inst(a, r);
     const EvInst& I = a.inst[i0];
@@ -1609,6 +1632,8 @@ constexpr int FIN_THREADS = 64;
  */
 __global__ void __launch_bounds__(FIN_THREADS) ev_finalize(EvArgs a) {
     __shared__ bool s_last;
+    nrdev::pdl_trigger();
+    nrdev::pdl_wait();
     for (uint64_t gc0 = (uint64_t)blockIdx.x * blockDim.x; gc0 < a.n_cells_total;
          gc0 += (uint64_t)gridDim.x * blockDim.x) {
         uint64_t gc = gc0 + threadIdx.x;
@@ -1714,7 +1739,8 @@ struct EventEngine::Impl {
     bool committed = false;
     int grid_blocks = 0;
     int pool_grid = 0;          /* resident blocks of the pool transport        */
-    /* ranged launch: every instance's tables fit shared memory */
+    /* ranged launches stage the tables in shared memory when every
+       instance's fit, else read them from global memory */
     bool ranged_fit = false;
     uint32_t range_built = 0;   /* range length d_range_begin was built for */
     uint32_t ranged_blocks = 0;
@@ -1729,6 +1755,10 @@ struct EventEngine::Impl {
     DBuf<unsigned long long> rb_base, rb_total;
     size_t smem_bytes = 0;
     bool one = true;
+    /* programmatic dependent launch between the generation's kernels (each
+       kernel's launch and prologue overlap the previous kernel's tail);
+       NRAPS_NO_PDL=1 in the environment turns it off */
+    bool pdl = !(std::getenv("NRAPS_NO_PDL") && std::getenv("NRAPS_NO_PDL")[0] == '1');
     ~Impl() { for (Inst* i : inst) delete i; }
 };
 
@@ -1858,7 +1888,7 @@ void set_smem_attr(size_t smem) {
 
 template <bool ONE, bool EXACT, bool BANK, bool REC>
 int launch_passes(const EvArgs& a, const EvParams& prm, int grid, size_t smem, uint64_t n_total,
-                  cudaStream_t s) {
+                  cudaStream_t s, bool pdl) {
     int launched = 0;
     uint32_t block = prm.block;
     smem += stage_bytes(block);
@@ -1867,16 +1897,18 @@ int launch_passes(const EvArgs& a, const EvParams& prm, int grid, size_t smem, u
     set_smem_attr<true, ONE, EXACT, BANK, REC>(smem);
     set_smem_attr<false, ONE, EXACT, BANK, REC>(smem);
     uint32_t P = prm.passes;
-    ev_pass<true, ONE, EXACT, BANK, REC><<<g0, block, smem, s>>>(a, 0, P == 0 ? 0xFFFFFFFFu : prm.K,
-                                                                 P == 0 ? 0u : prm.tail);
+    if (launch_k(pdl, ev_pass<true, ONE, EXACT, BANK, REC>, dim3(g0), dim3(block), smem, s, a, 0,
+                 P == 0 ? 0xFFFFFFFFu : prm.K, P == 0 ? 0u : prm.tail) != cudaSuccess)
+        return -1;
     ++launched;
     for (uint32_t p = 1; p <= P; ++p) {
         const bool last = p == P;
-        ev_pass<false, ONE, EXACT, BANK, REC><<<(unsigned)grid, block, smem, s>>>(
-            a, (int)p, last ? 0xFFFFFFFFu : prm.K, last ? 0u : prm.tail);
+        if (launch_k(pdl, ev_pass<false, ONE, EXACT, BANK, REC>, dim3((unsigned)grid), dim3(block), smem, s, a,
+                     (int)p, last ? 0xFFFFFFFFu : prm.K, last ? 0u : prm.tail) != cudaSuccess)
+            return -1;
         ++launched;
     }
-    return cudaPeekAtLastError() == cudaSuccess ? launched : -1;
+    return launched;
 }
 }  // namespace
 
@@ -1990,7 +2022,7 @@ int EventEngine::commit(cudaStream_t s, std::string& err) {
 
 int EventEngine::size_grid() {
     Impl& m = *impl_;
-    if (params.range && m.ranged_fit && m.range_built != params.range && m.committed) {
+    if (params.range && m.range_built != params.range && m.committed) {
         /* range prefix for params.range histories per block */
         const uint32_t n = (uint32_t)m.inst.size(), RL = params.range;
         std::vector<uint32_t> rb(n + 1, 0);
@@ -2072,7 +2104,7 @@ int EventEngine::enqueue_generation(cudaStream_t s, bool with_finalize, cudaEven
     if (t0) cudaEventRecord(t0, s);
     int r;
 #define EV_LAUNCH(ONE, EXACT, BANK, REC) \
-    r = launch_passes<ONE, EXACT, BANK, REC>(a, params, m.grid_blocks, ONE ? m.smem_bytes : 0, m.n_total, s)
+    r = launch_passes<ONE, EXACT, BANK, REC>(a, params, m.grid_blocks, ONE ? m.smem_bytes : 0, m.n_total, s, m.pdl)
     if (rec && m.one) {
         if (bank) { if (m.exact) EV_LAUNCH(true, true, true, true); else EV_LAUNCH(true, false, true, true); }
         else { if (m.exact) EV_LAUNCH(true, true, false, true); else EV_LAUNCH(true, false, false, true); }
@@ -2081,8 +2113,7 @@ int EventEngine::enqueue_generation(cudaStream_t s, bool with_finalize, cudaEven
            from global memory, as batched launches do */
         if (bank) { if (m.exact) EV_LAUNCH(false, true, true, true); else EV_LAUNCH(false, false, true, true); }
         else { if (m.exact) EV_LAUNCH(false, true, false, true); else EV_LAUNCH(false, false, false, true); }
-    } else if (params.range && params.passes == 0 && m.ranged_fit && m.range_built == params.range &&
-               (!bank || m.rb_ok)) {
+    } else if (params.range && params.passes == 0 && m.range_built == params.range && (!bank || m.rb_ok)) {
         ar.range_len = params.range;
         ar.range_begin = m.d_range_begin.p;
         if (bank) {
@@ -2091,13 +2122,24 @@ int EventEngine::enqueue_generation(cudaStream_t s, bool with_finalize, cudaEven
             ar.rb_chunk = m.rb_chunk.p; ar.rb_fill = m.rb_fill.p;
             ar.rb_base = m.rb_base.p; ar.rb_total = m.rb_total.p;
         }
-        const size_t rs = stage_bytes(params.block) + m.ranged_smem;
-        if (bank) {
-            if (m.exact) { set_smem_attr<true, 2, true, true, false>(rs); ev_pass<true, 2, true, true, false><<<m.ranged_blocks, params.block, rs, s>>>(ar, 0, 0xFFFFFFFFu, 0u); }
-            else { set_smem_attr<true, 2, false, true, false>(rs); ev_pass<true, 2, false, true, false><<<m.ranged_blocks, params.block, rs, s>>>(ar, 0, 0xFFFFFFFFu, 0u); }
+        if (m.ranged_fit) {
+            const size_t rs = stage_bytes(params.block) + m.ranged_smem;
+#define EV_RANGED(EXACT, BANK) \
+    set_smem_attr<true, 2, EXACT, BANK, false>(rs); \
+    launch_k(m.pdl, ev_pass<true, 2, EXACT, BANK, false>, dim3(m.ranged_blocks), dim3(params.block), rs, s, ar, 0, \
+             0xFFFFFFFFu, 0u)
+            if (bank) { if (m.exact) { EV_RANGED(true, true); } else { EV_RANGED(false, true); } }
+            else { if (m.exact) { EV_RANGED(true, false); } else { EV_RANGED(false, false); } }
+#undef EV_RANGED
         } else {
-            if (m.exact) { set_smem_attr<true, 2, true, false, false>(rs); ev_pass<true, 2, true, false, false><<<m.ranged_blocks, params.block, rs, s>>>(ar, 0, 0xFFFFFFFFu, 0u); }
-            else { set_smem_attr<true, 2, false, false, false>(rs); ev_pass<true, 2, false, false, false><<<m.ranged_blocks, params.block, rs, s>>>(ar, 0, 0xFFFFFFFFu, 0u); }
+            const size_t rs = stage_bytes(params.block);
+#define EV_RANGED(EXACT, BANK) \
+    set_smem_attr<true, 3, EXACT, BANK, false>(rs); \
+    launch_k(m.pdl, ev_pass<true, 3, EXACT, BANK, false>, dim3(m.ranged_blocks), dim3(params.block), rs, s, ar, 0, \
+             0xFFFFFFFFu, 0u)
+            if (bank) { if (m.exact) { EV_RANGED(true, true); } else { EV_RANGED(false, true); } }
+            else { if (m.exact) { EV_RANGED(true, false); } else { EV_RANGED(false, false); } }
+#undef EV_RANGED
         }
         r = cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
     } else if (m.one && m.pool_grid) {
@@ -2105,11 +2147,11 @@ int EventEngine::enqueue_generation(cudaStream_t s, bool with_finalize, cudaEven
         const unsigned pg = (unsigned)std::min<uint64_t>((m.n_total + params.pool - 1) / params.pool,
                                                          (uint64_t)m.pool_grid);
         if (bank) {
-            if (m.exact) ev_pool<true, true><<<pg ? pg : 1, POOL_THREADS, pdyn, s>>>(a, params.pool);
-            else ev_pool<false, true><<<pg ? pg : 1, POOL_THREADS, pdyn, s>>>(a, params.pool);
+            if (m.exact) launch_k(m.pdl, ev_pool<true, true>, dim3(pg ? pg : 1), dim3(POOL_THREADS), pdyn, s, a, params.pool);
+            else launch_k(m.pdl, ev_pool<false, true>, dim3(pg ? pg : 1), dim3(POOL_THREADS), pdyn, s, a, params.pool);
         } else {
-            if (m.exact) ev_pool<true, false><<<pg ? pg : 1, POOL_THREADS, pdyn, s>>>(a, params.pool);
-            else ev_pool<false, false><<<pg ? pg : 1, POOL_THREADS, pdyn, s>>>(a, params.pool);
+            if (m.exact) launch_k(m.pdl, ev_pool<true, false>, dim3(pg ? pg : 1), dim3(POOL_THREADS), pdyn, s, a, params.pool);
+            else launch_k(m.pdl, ev_pool<false, false>, dim3(pg ? pg : 1), dim3(POOL_THREADS), pdyn, s, a, params.pool);
         }
         r = cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
     } else if (m.one) {
@@ -2124,33 +2166,33 @@ int EventEngine::enqueue_generation(cudaStream_t s, bool with_finalize, cudaEven
     if (t1) cudaEventRecord(t1, s);
     int n = r;
     if (bank && ar.rb) {
-        ev_rb_scan<<<a.n_inst, RB_THREADS, 0, s>>>(ar);
+        launch_k(m.pdl, ev_rb_scan, dim3(a.n_inst), dim3(RB_THREADS), 0, s, ar);
         const size_t hb = ((size_t)ar.range_len + m.rb_hist_cells) * 4;
         if (hb > 48 * 1024) cudaFuncSetAttribute(ev_rb_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hb);
-        ev_rb_scatter<<<m.ranged_blocks, RB_THREADS, hb, s>>>(ar);
+        launch_k(m.pdl, ev_rb_scatter, dim3(m.ranged_blocks), dim3(RB_THREADS), hb, s, ar);
         n += 2;
     } else if (bank) {
-        int q = launch_exclusive_scan(m.count.p, m.n_total, m.block_sums.p, m.offsets.p, nullptr, s);
+        int q = launch_exclusive_scan(m.count.p, m.n_total, m.block_sums.p, m.offsets.p, nullptr, s, m.pdl);
         if (q < 0) return -1;
         n += q;
         if (a.hist_smem) {
             const size_t hb = (size_t)m.inst[0]->d.nc * 4;
             if (hb > 48 * 1024)
                 cudaFuncSetAttribute(ev_scatter_hist, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hb);
-            ev_scatter_hist<<<NSLAB * SCATTER_ONE_SPLIT, SCATTER_ONE_THREADS, hb, s>>>(a);
+            launch_k(m.pdl, ev_scatter_hist, dim3(NSLAB * SCATTER_ONE_SPLIT), dim3(SCATTER_ONE_THREADS), hb, s, a);
         } else if (m.one || rec) {
-            ev_scatter<SCAT_ONE><<<NSLAB * 8, 256, 0, s>>>(a);
+            launch_k(m.pdl, ev_scatter<SCAT_ONE>, dim3(NSLAB * 8), dim3(256), 0, s, a);
         } else if (a.n_inst <= SCAT_TAB_MAX) {
-            ev_scatter<SCAT_TAB><<<NSLAB * 8, 256, (size_t)a.n_inst * SCAT_TAB_BYTES, s>>>(a);
+            launch_k(m.pdl, ev_scatter<SCAT_TAB>, dim3(NSLAB * 8), dim3(256), (size_t)a.n_inst * SCAT_TAB_BYTES, s, a);
         } else {
-            ev_scatter<SCAT_DIRECT><<<NSLAB * 8, 256, 0, s>>>(a);
+            launch_k(m.pdl, ev_scatter<SCAT_DIRECT>, dim3(NSLAB * 8), dim3(256), 0, s, a);
         }
         ++n;
     }
     if (with_finalize) {
         unsigned gb = (unsigned)std::min<uint64_t>((m.n_cells_total + FIN_THREADS - 1) / FIN_THREADS,
                                                    (uint64_t)m.grid_blocks * 4);
-        ev_finalize<<<gb ? gb : 1, FIN_THREADS, 0, s>>>(ar);
+        launch_k(m.pdl, ev_finalize, dim3(gb ? gb : 1), dim3(FIN_THREADS), 0, s, ar);
         n += 1;
     }
     return cudaPeekAtLastError() == cudaSuccess ? n : -1;

@@ -70,6 +70,11 @@ def test_chained_generations(ctx_factory, case):
     r = ctx_factory(**opts).solve(p)
     want = _chained_k(p, opts, p.generations)
     assert np.array_equal(r.k64, want)
+    # ranged launches (tables staged, or read from global memory when they
+    # do not fit), each range ordering its own sites
+    rr = ctx_factory(range_len=700, **opts).solve(p)
+    assert np.array_equal(rr.k64, want)
+    np.testing.assert_allclose(rr.entropy, r.entropy, rtol=0, atol=1e-12)
     # the trace path on the same problem (records from the same kernels)
     grec, _, gs, gkq = ctx_factory(**opts).trace(p, 0, 1.0)
     wrec, _, ws, wkq = O.trace_woodcock(p, abi.make_opts(**opts), 0, 1.0)
