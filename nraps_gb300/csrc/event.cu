@@ -1517,6 +1517,23 @@ __device__ __forceinline__ double nlog2n(const EvArgs& a, uint32_t n) {
     return n < NLOG2N_TAB ? a.nlog2n[n] : (double)n * nr_log((double)n) * LOG2E;
 }
 
+/* the per-instance factors of a generation's fold: 1/N, 1/k, 1/(active
+   generations) and the power conversion times it (FP64 division is slow on
+   this part: a single-instance finalize block computes them once) */
+struct FoldK {
+    double inv_n, inv_k, fund, cf;
+    bool active;
+};
+__device__ __forceinline__ FoldK fold_factors(const EvInst& I, uint64_t gen, double k) {
+    FoldK f;
+    f.inv_n = 1.0 / (double)I.N;
+    f.inv_k = 1.0 / k;
+    f.fund = 1.0 / (double)(I.generations - I.skip);
+    f.cf = I.conv_const * f.fund;
+    f.active = gen >= I.skip;
+    return f;
+}
+
 /*
  * One cell of one instance at the end of a generation: reads and clears its
  * G tally bins and, in active generations, accumulates flux, flux moments
@@ -1525,7 +1542,7 @@ __device__ __forceinline__ double nlog2n(const EvArgs& a, uint32_t n) {
  * another is issued before the first store: the work is a few L2 round
  * trips, not arithmetic.
  */
-__device__ __forceinline__ void fold_cell(const EvInst& I, uint64_t c, uint64_t gen, double k) {
+__device__ __forceinline__ void fold_cell(const EvInst& I, uint64_t c, const FoldK& f) {
     const uint32_t G = I.G, nc = I.nc;
     double* __restrict__ tally = I.tally;
     double* __restrict__ flux_acc = I.flux_acc;
@@ -1533,11 +1550,11 @@ __device__ __forceinline__ void fold_cell(const EvInst& I, uint64_t c, uint64_t 
     double* __restrict__ flux_sq = I.flux_sq;
     const double inv_dx = I.inv_dx64[c];
     const uint32_t m = I.cmat[c];
-    const bool active = gen >= I.skip;
-    const double fund = 1.0 / (double)(I.generations - I.skip);
-    const double phi_scale = inv_dx / (double)I.N;         /* 1/(N dx)   */
-    const double flux_scale = phi_scale / k;                /* 1/(k N dx) */
-    const double acc_scale = flux_scale * (I.conv_const * k) * fund;
+    const bool active = f.active;
+    const double fund = f.fund;
+    const double phi_scale = inv_dx * f.inv_n;              /* 1/(N dx)   */
+    const double flux_scale = phi_scale * f.inv_k;          /* 1/(k N dx) */
+    const double acc_scale = phi_scale * f.cf;
     double fs = 0.0;
     for (uint32_t g0 = 0; g0 < G; g0 += 4) {
         double tl[4], nsf[4], fa[4], f1[4], f2[4];
@@ -1596,8 +1613,8 @@ __device__ void finish_instance(const EvArgs& a, uint32_t i, const double* h_giv
     if (gen >= I.skip) { st->ksum = ksum + k_new; st->ksum2 = ksum2 + k_new * k_new; st->nactive = nactive + 1; }
     unsigned int err = err0;
     if (a.bank) {
-        /* h holds -sum_c n_c log2(n_c) / B */
-        I.entropy[gen] = B ? nr_log((double)B) * LOG2E + h : 0.0;
+        /* h holds -sum_c n_c log2(n_c) */
+        I.entropy[gen] = B ? nr_log((double)B) * LOG2E + h / (double)B : 0.0;
         st->tot_sites = tot_sites + B;
         if (B > I.bank_cap) { B = I.bank_cap; err |= NR_ERR_CAPACITY; }
         st->n_bank = B;
@@ -1632,8 +1649,16 @@ constexpr int FIN_THREADS = 64;
  */
 __global__ void __launch_bounds__(FIN_THREADS) ev_finalize(EvArgs a) {
     __shared__ bool s_last;
+    __shared__ FoldK s_f;
     nrdev::pdl_trigger();
     nrdev::pdl_wait();
+    if (a.n_inst == 1) {
+        if (threadIdx.x == 0) {
+            const GenState* st = a.inst[0].st;
+            s_f = fold_factors(a.inst[0], st->gen, st->k);
+        }
+        __syncthreads();
+    }
     for (uint64_t gc0 = (uint64_t)blockIdx.x * blockDim.x; gc0 < a.n_cells_total;
          gc0 += (uint64_t)gridDim.x * blockDim.x) {
         uint64_t gc = gc0 + threadIdx.x;
@@ -1653,10 +1678,10 @@ __global__ void __launch_bounds__(FIN_THREADS) ev_finalize(EvArgs a) {
                 B = a.rb ? a.rb_total[inst] : a.offsets[I.hist_begin + I.N] - a.offsets[I.hist_begin];
             }
             if (gen < I.generations) {
-                fold_cell(I, c, gen, k);
+                fold_cell(I, c, a.n_inst == 1 ? s_f : fold_factors(I, gen, k));
                 if (a.bank) {
                     I.hist[c << I.hist_shift] = 0;
-                    if (cnt && B) h = -nlog2n(a, cnt) / (double)B;
+                    if (cnt && B) h = -nlog2n(a, cnt);
                 }
             }
         }
