@@ -432,11 +432,8 @@ __device__ __forceinline__ void move_down(Stage& sg, uint32_t from, uint32_t n, 
  * lanes, fly every live lane once per iteration, process real collisions,
  * stage fission sites and particles that completed K real collisions.
  */
-/* registers: 64 where the tables are in shared memory (one instance,
-   ranged); 80 where table pointers are global (batched, ranged over large
-   tables) */
 template <bool SOURCE, int ONE, bool EXACT, bool BANK, bool REC>
-__global__ void __launch_bounds__(256, (ONE == 1 || ONE == 2) ? 4 : 3) ev_pass(EvArgs a, int pass, uint32_t K, uint32_t tail) {
+__device__ __forceinline__ void ev_pass_body(const EvArgs& a, int pass, uint32_t K, uint32_t tail) {
     /* ONE: 0 batched (instances mixed in a warp), 1 one instance, 2 ranged
        (block b runs range b of one instance, that instance's tables staged
        in shared memory), 3 ranged with the tables read from global memory
@@ -857,6 +854,26 @@ __global__ void __launch_bounds__(256, (ONE == 1 || ONE == 2) ? 4 : 3) ev_pass(E
         if (lk) atomicAdd(&s->leaked, lk);
         if (cp) atomicAdd(&s->capped, cp);
     }
+}
+
+/* The transport kernels.  Registers: 56 for the persistent one-instance
+   transport (no spills; 9 blocks of 128 threads per SM instead of 8 measured
+   1-2% faster on single_large), 64 for ranged launches with the tables in
+   shared memory, 80 where table pointers are global (batched, ranged over
+   large tables). */
+template <bool SOURCE, int ONE, bool EXACT, bool BANK, bool REC>
+__global__ void __launch_bounds__(256, ONE == 2 ? 4 : 3) ev_pass(EvArgs a, int pass, uint32_t K, uint32_t tail) {
+    ev_pass_body<SOURCE, ONE, EXACT, BANK, REC>(a, pass, K, tail);
+}
+template <bool SOURCE, bool EXACT, bool BANK, bool REC>
+__global__ void __maxnreg__(56) ev_pass_one(EvArgs a, int pass, uint32_t K, uint32_t tail) {
+    ev_pass_body<SOURCE, 1, EXACT, BANK, REC>(a, pass, K, tail);
+}
+/* the kernel of one instantiation */
+template <bool SOURCE, int ONE, bool EXACT, bool BANK, bool REC>
+constexpr auto pass_kernel() {
+    if constexpr (ONE == 1) return &ev_pass_one<SOURCE, EXACT, BANK, REC>;
+    else return &ev_pass<SOURCE, ONE, EXACT, BANK, REC>;
 }
 
 /*
@@ -1905,7 +1922,7 @@ template <bool SOURCE, int ONE, bool EXACT, bool BANK, bool REC>
 void set_smem_attr(size_t smem) {
     static size_t granted = 48 * 1024;          /* the default dynamic limit         */
     if (smem > granted) {
-        cudaFuncSetAttribute(ev_pass<SOURCE, ONE, EXACT, BANK, REC>,
+        cudaFuncSetAttribute(pass_kernel<SOURCE, ONE, EXACT, BANK, REC>(),
                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         granted = smem;
     }
@@ -1922,13 +1939,13 @@ int launch_passes(const EvArgs& a, const EvParams& prm, int grid, size_t smem, u
     set_smem_attr<true, ONE, EXACT, BANK, REC>(smem);
     set_smem_attr<false, ONE, EXACT, BANK, REC>(smem);
     uint32_t P = prm.passes;
-    if (launch_k(pdl, ev_pass<true, ONE, EXACT, BANK, REC>, dim3(g0), dim3(block), smem, s, a, 0,
+    if (launch_k(pdl, pass_kernel<true, ONE, EXACT, BANK, REC>(), dim3(g0), dim3(block), smem, s, a, 0,
                  P == 0 ? 0xFFFFFFFFu : prm.K, P == 0 ? 0u : prm.tail) != cudaSuccess)
         return -1;
     ++launched;
     for (uint32_t p = 1; p <= P; ++p) {
         const bool last = p == P;
-        if (launch_k(pdl, ev_pass<false, ONE, EXACT, BANK, REC>, dim3((unsigned)grid), dim3(block), smem, s, a,
+        if (launch_k(pdl, pass_kernel<false, ONE, EXACT, BANK, REC>(), dim3((unsigned)grid), dim3(block), smem, s, a,
                      (int)p, last ? 0xFFFFFFFFu : prm.K, last ? 0u : prm.tail) != cudaSuccess)
             return -1;
         ++launched;
@@ -2089,9 +2106,9 @@ int EventEngine::size_grid() {
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     /* persistent grid: as many blocks as are resident at once */
     int per_sm = 0;
-    const void* fn = m.one ? (m.exact ? (const void*)ev_pass<false, true, true, true, false>
-                                      : (const void*)ev_pass<false, true, false, true, false>)
-                           : (const void*)ev_pass<false, false, false, true, false>;
+    const void* fn = m.one ? (m.exact ? (const void*)pass_kernel<false, 1, true, true, false>()
+                                      : (const void*)pass_kernel<false, 1, false, true, false>())
+                           : (const void*)pass_kernel<false, 0, false, true, false>();
     const size_t dyn = stage_bytes(params.block) + (m.one ? m.smem_bytes : 0);
     if (dyn > 48 * 1024) cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, (int)params.block, dyn) != cudaSuccess ||
