@@ -449,6 +449,8 @@ int read_state(nraps_session* s, GenState& g) {
 }
 
 int state_status(nraps_session* s, const GenState& g) {
+    if (g.error & NR_ERR_STALLED)
+        return set_err(s->ctx, NRAPS_ERR_CUDA, "a bounded device wait ran out (a range's chunk id)");
     if (g.error & NR_ERR_CAPACITY)
         return set_err(s->ctx, NRAPS_ERR_CAPACITY, "fission bank overflowed its capacity (raise opts.bank_factor)");
     if (g.error & NR_ERR_EMPTY)

@@ -25,6 +25,7 @@
 #define NR_ERR_CAPACITY 1u    /* GenState.error bits                        */
 #define NR_ERR_EMPTY    2u
 #define NR_ERR_CAPPED   4u
+#define NR_ERR_STALLED  8u    /* a bounded device wait ran out              */
 
 struct GenState {
     uint64_t gen;             /* generation being run                        */

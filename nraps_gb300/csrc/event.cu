@@ -378,11 +378,12 @@ __device__ __forceinline__ bool flush_sites(const EvArgs& a, S& sg, uint32_t n, 
    (warp-wide; ranged launches, block b = range b).  The warp whose
    reservation holds the first slot of a chunk takes that chunk from the pool
    and publishes its id in shared memory; a warp that reaches a chunk first
-   waits for the id (bounded).  Returns false (all lanes) when the range or
-   the pool is full or the wait ran out. */
+   waits for the id (bounded; a wait that runs out sets NR_ERR_STALLED in
+   *err).  Returns false (all lanes) when the range or the pool is full or
+   a wait ran out. */
 template <class S>
 __device__ __forceinline__ bool flush_range_sites(const EvArgs& a, S& sg, uint32_t n, uint32_t lane,
-                                                  uint32_t* s_fill, volatile uint32_t* s_chunk) {
+                                                  uint32_t* s_fill, volatile uint32_t* s_chunk, unsigned int* err) {
     uint32_t p0 = 0;
     if (lane == 0) {
         p0 = atomicAdd(s_fill, n);
@@ -405,6 +406,7 @@ __device__ __forceinline__ bool flush_range_sites(const EvArgs& a, S& sg, uint32
             __nanosleep(64);
             id = s_chunk[c];
         }
+        if (id == RB_UNSET) atomicOr(err, NR_ERR_STALLED);
         ok = id < RB_FULL;
         if (ok) a.sites[(uint64_t)id * RB_CHUNK + (pos & (RB_CHUNK - 1))] = sg.site[lane];
     }
@@ -772,7 +774,7 @@ __device__ __forceinline__ void ev_pass_body(const EvArgs& a, int pass, uint32_t
                 staged_sites += __popc(sm);
                 __syncwarp();
                 if (staged_sites >= 32) {
-                    const bool fl = rbk ? flush_range_sites(a, sg, 32, lane, &s_rfill, s_rchunk)
+                    const bool fl = rbk ? flush_range_sites(a, sg, 32, lane, &s_rfill, s_rchunk, &Ip->st->error)
                                         : flush_sites(a, sg, 32, slab, lane);
                     if (!fl) slab_full = true;
                     move_down(sg, 32, staged_sites - 32, lane, true);
@@ -831,7 +833,7 @@ __device__ __forceinline__ void ev_pass_body(const EvArgs& a, int pass, uint32_t
     if (!ONE && kq_part) atomicAdd(&a.inst[kq_inst].st->kq, kq_part);
     if (staged) flush_particles(a, sg, staged, pass, qout, lane);
     if (BANK && staged_sites) {
-        const bool fl = rbk ? flush_range_sites(a, sg, staged_sites, lane, &s_rfill, s_rchunk)
+        const bool fl = rbk ? flush_range_sites(a, sg, staged_sites, lane, &s_rfill, s_rchunk, &Ip->st->error)
                             : flush_sites(a, sg, staged_sites, slab, lane);
         if (!fl) slab_full = true;
     }

@@ -210,6 +210,7 @@ int nraps_batch_sync(nraps_batch* b) {
     for (size_t i = 0; i < b->buf.size(); ++i) {
         GenState g;
         CK(cudaMemcpy(&g, b->buf[i]->st, sizeof g, cudaMemcpyDeviceToHost));
+        if (g.error & NR_ERR_STALLED) return set_err(ctx, NRAPS_ERR_CUDA, "instance " + std::to_string(i) + ": a bounded device wait ran out");
         if (g.error & NR_ERR_CAPACITY) return set_err(ctx, NRAPS_ERR_CAPACITY, "instance " + std::to_string(i) + ": fission bank overflowed");
         if (g.error & NR_ERR_EMPTY) return set_err(ctx, NRAPS_ERR_EMPTY_BANK, "instance " + std::to_string(i) + ": fission bank empty");
         if (g.error & NR_ERR_CAPPED) return set_err(ctx, NRAPS_ERR_CAPPED, "instance " + std::to_string(i) + ": event cap reached");
@@ -445,7 +446,8 @@ int nraps_server_step(nraps_server* s, uint32_t* n_running, uint32_t* n_finished
         if (err_bits || converged || capped) {
             q.state = NRAPS_REQ_DONE;
             q.t_done = t;
-            q.status = err_bits ? ((g.error & NR_ERR_CAPACITY) ? NRAPS_ERR_CAPACITY
+            q.status = err_bits ? ((g.error & NR_ERR_STALLED) ? NRAPS_ERR_CUDA
+                                   : (g.error & NR_ERR_CAPACITY) ? NRAPS_ERR_CAPACITY
                                    : (g.error & NR_ERR_EMPTY) ? NRAPS_ERR_EMPTY_BANK : NRAPS_ERR_CAPPED)
                                 : NRAPS_OK;
             s->ev.remove_instance((uint32_t)i);
