@@ -18,7 +18,17 @@
  * that completed K real collisions and new fission sites are staged per warp
  * in shared memory and flushed 32 at a time with one atomic each.
  * Single-instance launches stage the instance's tables in shared memory;
- * batched launches read each particle's instance tables through L1.
+ * batched launches read each particle's instance tables through L1; ranged
+ * launches give each block a range of one instance's histories (its tables
+ * staged, or read from global memory when they do not fit).
+ *
+ * Fission-bank order (parent, seq): persistent launches flush sites into 128
+ * slabs, then the per-history site counts are scanned and every site is
+ * scattered to offsets[parent] + seq; ranged launches append a range's sites
+ * to chunks of a shared pool and order each range on its own (ev_rb_scan,
+ * ev_rb_scatter).  Every kernel of a generation is launched with
+ * programmatic stream serialization and waits (griddepcontrol) before
+ * touching what the kernel before it produced.
  */
 #include <algorithm>
 #include <cstdlib>

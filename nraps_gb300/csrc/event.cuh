@@ -10,7 +10,8 @@
  *               the survivors are compacted into the other queue;
  *   drain       the last queue runs to completion;
  *   bank        exclusive scan of per-history site counts, then the
- *               unordered sites are scattered to (parent, sequence) order;
+ *               unordered sites are scattered to (parent, sequence) order
+ *               (ranged launches: each range orders its own sites);
  *   finalize    per-cell FP64 flux/fission-source accumulation, Shannon
  *               entropy, and per-instance k, bank size and generation index.
  * Every particle owns a PCG32 stream (seed of its instance and generation,
