@@ -135,18 +135,33 @@ class Clocks:
                 "samples": len(sm)}
 
 
-def make_workload(name: str, seed: int, warmup: int, steps: int):
+def full_workload(name: str, seed: int):
+    """The workload as configured (its own histories and inactive + active
+    generations)."""
     from nraps_gb300 import synth
     if name == "single_large":
-        p = synth.single_large(seed)
-    elif name == "plain_small":
-        p = synth.plain_small(seed)
-    elif name == "scale_stress":
-        p = synth.scale_stress(seed)
-    else:
-        raise SystemExit(f"unknown workload {name}")
-    p = p.with_(generations=warmup + steps, skip=warmup)
-    return p
+        return synth.single_large(seed)
+    if name == "plain_small":
+        return synth.plain_small(seed)
+    if name == "scale_stress":
+        return synth.scale_stress(seed)
+    raise SystemExit(f"unknown workload {name}")
+
+
+def make_workload(name: str, seed: int, warmup: int, steps: int):
+    """The workload with warm-up steps as inactive and timed steps as active
+    generations."""
+    return full_workload(name, seed).with_(generations=warmup + steps, skip=warmup)
+
+
+def arm_config(args, prob, world: int) -> dict:
+    """The `config` object of the JSON line: the workload, the same for both
+    arms."""
+    return {"workload": args.workload, "histories_per_step": prob.histories,
+            "cells": prob.n_cells, "groups": prob.energygroups,
+            "generations": f"{args.warmup} inactive (warm-up) + {args.steps} active (timed)",
+            "l2": "flushed between steps (256 MB write)",
+            "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"}
 
 
 ARMS = {
@@ -210,7 +225,10 @@ def measure_device(prob, arm: str, steps: int, warmup: int, seed: int, device: i
 
 
 def measure_e2e(prob, arm: str, seed: int, device: int):
-    """The drop-in call with host buffers: nraps_monte_carlo end to end."""
+    """The drop-in call with host buffers: nraps_monte_carlo end to end over
+    the workload's whole run (single_large: 50 inactive + 200 active
+    generations, whatever --steps/--warmup say), uploads, tuning and
+    downloads inside the timed region."""
     from nraps_gb300 import api
     ctx = api.Context(seed=seed, device=device, **ARMS[arm])
     # warm-up: one untimed call of the same size (module loading, the
@@ -229,7 +247,81 @@ def measure_e2e(prob, arm: str, seed: int, device: int):
            + r.k64.nbytes + r.entropy.nbytes + r.flux_mean.nbytes + r.flux_sem.nbytes)
     g = prob.generations
     return dict(value=prob.histories * g / dt, seconds=dt, h2d=h2d / g, d2h=d2h / g, k_mean=r.stats.k_mean,
-                k_sigma=r.stats.k_sigma)
+                k_sigma=r.stats.k_sigma, generations=g)
+
+
+def measure_parity(full, seed: int, device: int, plain_active: int = 100, event_batch: int = 20,
+                   plain_batch: int = 10, plain_ms_per_generation: float | None = None,
+                   event_ms_per_generation: float | None = None, coarse: int = 1):
+    """The chosen form (event Woodcock, FP32 flights) against the plain FP64
+    kernel on the same workload and seeds, BANK mode both: k difference with
+    a batch-means sigma, per-group flux chi^2 and integrated-flux bias, and
+    the wall time each form needs to reach sigma_k <= 50 pcm."""
+    from nraps_gb300 import api, parity
+    runs = {}
+    for arm, active, batch in (("event", full.generations - full.skip, event_batch),
+                               ("plain", plain_active, plain_batch)):
+        p = full.with_(generations=full.skip + active)
+        ctx = api.Context(seed=seed, device=device, **ARMS[arm])
+        s = ctx.session(p)
+        runs[arm] = parity.run_batches(s, p, batch)
+        runs[arm]["generations"] = p.generations
+        s.close()
+        ctx.close()
+    G, nc, skip = full.energygroups, full.n_cells, full.skip
+    c = parity.compare(runs["event"], runs["plain"], G, nc, skip, coarse=coarse)
+    c["workload"] = full.name.split(":")[0]
+    c["event"] = {"generations": f"{skip} + {runs['event']['generations'] - skip}",
+                  "batch": event_batch, "k_mean": c.pop("k_a"), "sigma_pcm": c.pop("sigma_a_pcm")}
+    c["plain_fp64"] = {"generations": f"{skip} + {runs['plain']['generations'] - skip}",
+                       "batch": plain_batch, "k_mean": c.pop("k_b"), "sigma_pcm": c.pop("sigma_b_pcm")}
+    for arm, key, ms in (("event", "event", event_ms_per_generation),
+                         ("plain", "plain_fp64", plain_ms_per_generation)):
+        if ms:
+            c[key]["time_to_50pcm"] = parity.time_to_sigma(runs[arm]["k64"][skip:], ms, skip)
+    c["same_seeds"] = True
+    c["mode"] = "BANK"
+    return c
+
+
+def measure_plain_small(seed: int, device: int, threads: int):
+    """Config 0 (plain_small: 4 groups, 500 cells, 10k histories, 50 + 100
+    generations) on the host cores (the oracle, COMPAT f32, the reference's
+    thread policy) and on the plain FP64 GPU kernel (COMPAT, the same
+    algorithm, and BANK): histories/s, k, sigma_k and time to 50 pcm."""
+    from nraps_gb300 import abi, api, parity, synth
+    from oracle import oracle as O
+    p = synth.plain_small(seed)
+    skip, active = p.skip, p.generations - p.skip
+    out = {"workload": "plain_small", "cells": p.n_cells, "groups": p.energygroups,
+           "histories_per_generation": p.histories, "generations": f"{skip} + {active}"}
+    o = abi.make_opts(seed=12345, mode=abi.MODE_COMPAT, precision=abi.PREC_FP32, compat_threads=threads)
+    t = time.perf_counter()
+    r = O.monte_carlo(p, o, threads=threads, acc64=False)
+    dt = time.perf_counter() - t
+    k = r.k64[skip:]
+    out["cpu_port_compat_f32"] = {
+        "histories_per_s": (p.histories + threads) * p.generations / dt, "seconds": dt, "cores": threads,
+        "k_mean": float(k.mean()), "sigma_pcm": parity.naive_sigma(k) * 1e5,
+        "time_to_50pcm": parity.time_to_sigma(k, 1000.0 * dt / p.generations, skip)}
+    for name, mode in (("gpu_plain_fp64_compat", abi.MODE_COMPAT), ("gpu_plain_fp64_bank", abi.MODE_BANK)):
+        ctx = api.Context(seed=12345, device=device, mode=mode, precision=abi.PREC_FP64,
+                          compat_threads=threads if mode == abi.MODE_COMPAT else 0)
+        ctx.solve(p.with_(generations=4, skip=2))          # module load, first allocations
+        s = ctx.session(p)
+        s.set_profile(True)
+        s.run(p.generations)
+        tm = s.timing()
+        res = s.results()
+        s.close()
+        ctx.close()
+        k = res.k64[skip:]
+        ms_gen = tm["total_ms"] / p.generations
+        hist = (p.histories + (threads if mode == abi.MODE_COMPAT else 0)) * p.generations
+        out[name] = {"histories_per_s": hist / (tm["total_ms"] / 1000.0), "ms_per_generation": ms_gen,
+                     "k_mean": float(k.mean()), "sigma_pcm": parity.naive_sigma(k) * 1e5,
+                     "time_to_50pcm": parity.time_to_sigma(k, ms_gen, skip)}
+    return out
 
 
 def measure_batched(seed: int, device: int, steps: int, warmup: int = 3):
@@ -329,14 +421,19 @@ def run_reference_arm(args):
     for _ in range(args.steps):
         O.monte_carlo(q, o, threads=threads, acc64=False, max_generations=1)
     dt = time.perf_counter() - t
+    # the reference simulates N + T histories per generation (start..=end
+    # per thread, src/mc_code.rs:226,302-307): all of them count as work
     hist = (n + threads) * args.steps
     value = hist / dt
-    sample = (f"{args.steps} generations of {n}+{threads} histories of {args.workload} "
-              f"(COMPAT f32, CPU restatement of src/mc_code.rs)")
+    sample = (f"{args.steps} generations of {n}+{threads} histories sampled from {args.workload} "
+              f"({prob.histories} histories per generation; COMPAT f32, CPU restatement of "
+              f"src/mc_code.rs, the reference's thread policy)")
+    world = int(os.environ.get("WORLD_SIZE", "1"))
     line = {"impl": "reference", "metric": "histories/s", "value": value, "unit": "histories/s",
             "n_gpus": 0, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * dt / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic", "config": {"workload": args.workload, "histories_per_step": n + threads},
+            "data": "synthetic", "config": arm_config(args, prob, world),
+            "form": "reference algorithm on the host cores (COMPAT, f32)",
             "cpu_baseline": {"value": value, "unit": "histories/s", "cores": threads, "kind": "port",
                              "sample": sample},
             "e2e": {"value": value, "unit": "histories/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -350,7 +447,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=50)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="single_large")
-    ap.add_argument("--arm", default="auto", choices=["auto", "event", "plain"])
+    ap.add_argument("--arm", default="event", choices=["event", "plain"])
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--plain-steps", type=int, default=5)
     ap.add_argument("--cpu-budget-s", type=float, default=12.0)
@@ -366,6 +463,9 @@ def main():
     ap.add_argument("--initial-source", type=int, default=0, help="1 = start from the diffusion fission source")
     ap.add_argument("--range", type=int, default=0, help="ranged launches of this many histories (profiling)")
     ap.add_argument("--scale-stress", type=int, default=1, help="1 = also run the 10M-history, 200k-cell slab")
+    ap.add_argument("--parity", type=int, default=1,
+                    help="1 = event FP32 vs plain FP64 on the full workload (k, flux chi^2, time to 50 pcm)")
+    ap.add_argument("--plain-small", type=int, default=1, help="1 = also run config 0 (CPU port vs plain FP64)")
     args = ap.parse_args()
     if args.warmup < 3:
         raise SystemExit("--warmup must be >= 3")
@@ -385,15 +485,8 @@ def main():
     seed = replica_seed(args.seed, rank)
     prob = make_workload(args.workload, args.seed, args.warmup, args.steps)
 
+    # no fallback: if the chosen form cannot run, the bench fails
     arm = args.arm
-    if arm == "auto":
-        arm = "event"
-        try:
-            c = api.Context(seed=1, device=local, **ARMS["event"])
-            c.solve(prob.with_(histories=1000, generations=2, skip=1))
-            c.close()
-        except api.NrapsError:
-            arm = "plain"
     clocks = Clocks(local)
     if world > 1:
         torch.distributed.barrier()
@@ -419,15 +512,27 @@ def main():
         dp = measure_device(pp, "plain", args.plain_steps, 3, seed, local)
         plain = {"histories_per_s": dp["histories"] / (dp["ms"] / 1000.0),
                  "collisions_per_s": dp["collisions"] / (dp["ms"] / 1000.0),
-                 "steps": args.plain_steps, "dtype": "f64"}
+                 "ms_per_step": dp["ms"] / args.plain_steps, "steps": args.plain_steps, "dtype": "f64",
+                 "k_mean": dp["k_mean"], "sigma_k_pcm": dp["k_sigma"] * 1e5}
 
+    full = full_workload(args.workload, args.seed)
     e2e = None
     if not args.no_e2e:
-        e = measure_e2e(prob, arm, seed, local)
+        e = measure_e2e(full, arm, seed, local)
         e_sec = max_over_ranks(e["seconds"], f"cuda:{local}")
-        e2e = {"value": replica_throughput(prob.histories * prob.generations, 1000.0 * e_sec, world),
+        e2e = {"value": replica_throughput(full.histories * full.generations, 1000.0 * e_sec, world),
                "unit": "histories/s", "h2d_bytes_per_step": e["h2d"],
-               "d2h_bytes_per_step": e["d2h"], "seconds": e_sec, "call": "nraps_monte_carlo"}
+               "d2h_bytes_per_step": e["d2h"], "seconds": e_sec, "call": "nraps_monte_carlo",
+               "generations_per_call": e["generations"], "k_mean": e["k_mean"],
+               "sigma_k_pcm": e["k_sigma"] * 1e5}
+
+    fp = None
+    if arm == "event" and args.parity and rank == 0:
+        fp = measure_parity(full, seed, local, event_ms_per_generation=ms / args.steps,
+                            plain_ms_per_generation=plain["ms_per_step"] if plain else None)
+        if plain:
+            plain["k_mean"], plain["sigma_k_pcm"] = fp["plain_fp64"]["k_mean"], fp["plain_fp64"]["sigma_pcm"]
+            plain["k_from"] = f"fp32_vs_fp64 run ({fp['plain_fp64']['generations']} generations)"
 
     peak, peak_kind = peaks()
     per_launch_ms = d["transport_ms"] / max(1, d["transport_launches"])
@@ -437,6 +542,9 @@ def main():
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "peak_kind": peak_kind,
                 "traffic": (tpc * coll_per_launch) if tpc else None,
+                "traffic_source": ("DRAM bytes per real collision from the ncu capture in "
+                                   "profiles/traffic_event_single_large.txt x this run's real collisions "
+                                   "per launch") if tpc else None,
                 "kernel": "event_transport" if arm == "event" else "plain_transport",
                 "bytes_per_collision": ALG_BYTES_PER_COLLISION,
                 "launches": d["transport_launches"], "avg_launch_ms": per_launch_ms}
@@ -455,6 +563,8 @@ def main():
                "sample": f"1 generation of {n}+{threads} histories of {args.workload}, COMPAT f32, "
                          f"CPU restatement of src/mc_code.rs (reference thread policy)"}
 
+    small = (measure_plain_small(args.seed, local, max(1, (os.cpu_count() or 2) - 1))
+             if args.plain_small and rank == 0 else None)
     batched = measure_batched(args.seed, local, args.batched_steps) if args.batched_steps > 0 and arm == "event" else None
     scale = measure_scale_stress(args.seed, local) if args.scale_stress and arm == "event" else None
     serving = (measure_serving(args.seed, local, args.serve_seconds, args.serve_rate)
@@ -466,16 +576,14 @@ def main():
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32+f64" if arm == "event" else "f64", "data": "synthetic",
-            "config": {"workload": args.workload, "histories_per_step": prob.histories,
-                       "cells": prob.n_cells, "groups": prob.energygroups,
-                       "generations": f"{args.warmup} inactive (warm-up) + {args.steps} active (timed)",
-                       "form": "event Woodcock FP32 flights + FP64 tallies" if arm == "event"
-                       else "plain history-per-thread FP64", "l2": "flushed between steps (256 MB write)",
-                       "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
+            "config": arm_config(args, prob, world),
+            "form": "event Woodcock FP32 flights + FP64 tallies" if arm == "event"
+            else "plain history-per-thread FP64",
             "sigma_k_pcm": d["k_sigma"] * 1e5, "k_mean": d["k_mean"],
             "collisions_per_s": world * d["collisions"] / (ms / 1000.0),
             "gpu_launches": d["launches"], "launch_shape": d["tuning"],
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "plain": plain, "clocks": clk,
+            "fp32_vs_fp64": fp, "plain_small": small,
             "batched": batched, "serving": serving, "scale_stress": scale,
         }
         print(json.dumps(line), flush=True)

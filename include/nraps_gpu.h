@@ -402,9 +402,12 @@ void nraps_server_destroy(nraps_server* s);
    MatTypes*EnergyGroups <= 1024, MatTypes*EnergyGroups^2 <= 16384,
    EnergyGroups <= 16; larger problems are rejected with NRAPS_ERR_INVALID.
    The first call on a device looks up the array's device address; make it
-   before any stream capture.  Calls share the array: calls whose work
-   overlaps on the GPU race, so order them.  The call checks the device inputs
-   (one synchronisation of `stream`), then enqueues the generation and returns;
+   before any stream capture.  Every call checks the device inputs and waits
+   for that check (one synchronisation of `stream`), so no call can be made
+   while `stream` is being captured.  Calls share the array: calls whose work
+   overlaps on the GPU race, so order them; the race includes the input check
+   (an overlapping call can make another call fail on its inputs, or pass
+   with bad ones).  After the check the call enqueues the generation and returns;
    d_error (may be NULL) receives the generation's error bits (4 = a history
    hit max_events).  Errors are reported through nraps_last_error(NULL). */
 typedef struct nraps_device_problem {

@@ -18,12 +18,18 @@
  * the host is only a stand-in.  The device address is looked up once per
  * device with cudaGetSymbolAddress, with that device current, on the first
  * call made on that device; make that first call before any stream capture.
+ * Every call also waits for its input check on the caller's stream (one copy
+ * into host memory and a stream synchronisation), so no call can be made
+ * while that stream is being captured.
  *
  * Every call shares the one array and the previous call's contents remain in
  * it.  Each call rewrites the tables and clears the counters before its
  * kernels run, on the caller's stream.  Two calls whose work overlaps on the
  * GPU (different streams, or several host threads) race on the array: the
- * caller must order them.
+ * caller must order them.  The race covers the input check too: an
+ * overlapping call can clear or set the flags between another call's check
+ * and its read, so that call may be rejected for the other's inputs or pass
+ * with bad ones of its own.
  */
 #include <cuda_runtime.h>
 
@@ -54,6 +60,10 @@ unsigned char* g_addr[MAX_DEVICES] = {nullptr};
 #define NOALLOC_BAD_FUEL 2u
 
 struct Flags { unsigned int bad; };
+
+/* the state and the flags must fit the 256-byte header ahead of the tables */
+static_assert(sizeof(GenState) + sizeof(Flags) <= 256, "GenState and Flags outgrew the array's header");
+static_assert(NOALLOC_BYTES % alignof(float) == 0 && 256 % alignof(GenState) == 0, "table alignment");
 
 /* derived tables (same arithmetic as the packed FP32 tables), cleared state,
    and a range check of the device inputs into the (pre-cleared) flags */

@@ -12,10 +12,10 @@ is a copy of the fuel, unused), so MatTypes = 3.
 "Deterministic k" is defined by `diffusion_k`: FP64 multigroup diffusion,
 cell-centred finite differences on the tally mesh, Marshak vacuum boundaries
 (or zero-current for reflective ones), the full multigroup loss operator
-factorised once, and a power iteration on the fission source.  The 12,500 cm scale_stress slab uses
-`infinite_k` (k-infinity of the volume-homogenised slab): leakage is
-negligible there and a power iteration on 200,000 cells would not converge
-in reasonable time.
+factorised once, and a power iteration on the fission source.  The 12,500 cm
+scale_stress slab has a dominance ratio so close to one that a power
+iteration crawls; `diffusion_k_large` finds the same eigenvalue with Arnoldi
+iterations on a cell-major, banded factorisation.
 
 Workloads (1D slab, vacuum boundaries unless stated):
   plain_small     4 groups, 10 fuel regions of 1.0 cm alternating with 11 water
@@ -138,6 +138,54 @@ def diffusion_k(mat, dx, xs, sigf, boundl=0.0, boundr=0.0, tol=1e-9, max_outer=5
     return float(k)
 
 
+def diffusion_k_large(mat, dx, xs, sigf, boundl=0.0, boundr=0.0, tol=1e-9):
+    """The same diffusion k as `diffusion_k` for slabs too long for a power
+    iteration (the 12,500 cm scale-stress slab: its dominance ratio is so
+    close to one that hundreds of outer iterations barely move k): unknowns
+    ordered cell-major, so the loss operator is block tridiagonal with G x G
+    blocks and its LU keeps to the band; the dominant eigenvalue of
+    loss^-1 * fission found by implicitly restarted Arnoldi (ARPACK)."""
+    from scipy.sparse import coo_matrix
+    from scipy.sparse.linalg import LinearOperator, eigs, splu
+    M, G = xs["M"], xs["G"]
+    mat = np.asarray(mat, np.int64)
+    h = np.asarray(dx, np.float64)
+    n = h.size
+    sigt = xs["sigt"]; scat = xs["scat"]; chi = xs["chi"]
+    rows, cols, vals = [], [], []
+    nsf = np.zeros((n, G)); chic = np.zeros((n, G))
+    i = np.arange(n)
+    for g in range(G):
+        idx = mat + M * g
+        D = 1.0 / (3.0 * sigt[idx])
+        dc = 2.0 * D[:-1] * D[1:] / (h[:-1] * D[1:] + h[1:] * D[:-1])
+        diag = (sigt[idx] - scat[G * G * mat + G * g + g]) * h
+        diag[:-1] += dc
+        diag[1:] += dc
+        diag[0] += 0.0 if boundl > 0 else 2.0 * D[0] / (4.0 * D[0] + h[0])
+        diag[-1] += 0.0 if boundr > 0 else 2.0 * D[-1] / (4.0 * D[-1] + h[-1])
+        rows += [i * G + g, i[:-1] * G + g, i[1:] * G + g]
+        cols += [i * G + g, i[1:] * G + g, i[:-1] * G + g]
+        vals += [diag, -dc, -dc]
+        for gp in range(G):                       # in-scatter gp -> g
+            if gp != g:
+                rows.append(i * G + g); cols.append(i * G + gp)
+                vals.append(-scat[G * G * mat + G * gp + g] * h)
+        nsf[:, g] = NU * sigf[idx]
+        chic[:, g] = chi[idx]
+    A = coo_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))),
+                   shape=(G * n, G * n)).tocsc()
+    lu = splu(A, permc_spec="NATURAL")
+
+    def apply(x):
+        fs = (nsf * x.reshape(n, G)).sum(1) * h
+        return lu.solve((chic * fs[:, None]).reshape(-1))
+
+    op = LinearOperator((G * n, G * n), matvec=apply, dtype=np.float64)
+    w = eigs(op, k=1, which="LM", tol=tol, v0=np.ones(G * n), ncv=40, return_eigenvectors=False)
+    return float(w[0].real)
+
+
 def _mesh_from_regions(region_mat, region_width, cells_per_region):
     mats, dxs, lefts, rights = [], [], [], []
     left = np.float32(0.0)
@@ -175,15 +223,19 @@ def infinite_k(mats, dxs, xs, sigf):
 
 
 def _scale_fission(xs, mats, dxs, boundl, boundr, method="diffusion"):
+    """sigf = shape / k(shape), clamped at siga: the diffusion k of the slab is
+    then 1 (recomputed when the clamp bites).  k is linear in a common scale
+    of sigf, so one eigenvalue solve sets it."""
     shape = xs["sigf_shape"]
     if method == "infinite":
         k1 = infinite_k(mats, dxs, xs, shape)
         sigf = np.minimum(shape / k1, xs["siga"])
         return sigf, infinite_k(mats, dxs, xs, sigf)
-    k1 = diffusion_k(mats, dxs, xs, shape, boundl, boundr)
+    solve = diffusion_k_large if method == "diffusion_large" else diffusion_k
+    k1 = solve(mats, dxs, xs, shape, boundl, boundr)
     sigf = shape / k1
     sigf = np.minimum(sigf, xs["siga"])
-    k = diffusion_k(mats, dxs, xs, sigf, boundl, boundr) if np.any(sigf < shape / k1) else 1.0
+    k = solve(mats, dxs, xs, sigf, boundl, boundr) if np.any(sigf < shape / k1) else 1.0
     return sigf, k
 
 
@@ -275,10 +327,19 @@ def batched(seed: int = 1, n: int = 256, cells_per_region: int = 10, inactive: i
     return out
 
 
+_SCALE_STRESS = {}
+
+
 def scale_stress(seed: int = 1, histories: int = 10_000_000) -> ProblemArrays:
-    rng = np.random.default_rng(seed)
-    return random_slab(rng, 10_000, 8, 0.5, 2.0, 20, histories, 20, 50, k_method="infinite",
-                       name="scale_stress: 8 groups, 10000 regions, 200000 cells, 10M histories, 20+50")
+    """nu*sigf scaled by the slab's diffusion k (Arnoldi on the 1.6M-unknown
+    operator, ~15 s; cached per seed within a process)."""
+    if seed not in _SCALE_STRESS:
+        rng = np.random.default_rng(seed)
+        _SCALE_STRESS[seed] = random_slab(
+            rng, 10_000, 8, 0.5, 2.0, 20, 10_000_000, 20, 50, k_method="diffusion_large",
+            name="scale_stress: 8 groups, 10000 regions, 200000 cells, 10M histories, 20+50")
+    p = _SCALE_STRESS[seed]
+    return p if histories == p.histories else p.with_(histories=histories)
 
 
 def write_input_file(p: ProblemArrays, path: str, solution: int = 1) -> None:
