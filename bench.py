@@ -212,7 +212,7 @@ def measure_device(prob, arm: str, steps: int, warmup: int, seed: int, device: i
                transport_ms=t1["transport_ms"] - t0["transport_ms"],
                transport_launches=t1["transport_launches"] - t0["transport_launches"],
                launches=ctx.launches - launches0, k_mean=res.stats.k_mean, k_sigma=res.stats.k_sigma,
-               tuning=tuning)
+               tuning=tuning, k64=res.k64.copy())
     # the flush zero_() launches are torch's, not ours; ctx.launches counts ours
     s.close()
     ctx.close()
@@ -358,29 +358,48 @@ def measure_serving(seed: int, device: int, seconds: float, rate: float):
     return r
 
 
-def measure_scale_stress(seed: int, device: int):
-    """8 groups, 10,000 regions, 200,000 cells, 10M histories, 20 + 50."""
-    from nraps_gb300 import synth
+def measure_scale_stress(seed: int, device: int, plain_active: int = 20):
+    """8 groups, 10,000 regions, 200,000 cells, 10M histories, 20 + 50, nu*sigf
+    scaled so the slab's diffusion k is 1.  Both forms start from the
+    diffusion fission source (a 12,500 cm slab's dominance ratio is so close
+    to one that 20 inactive generations cannot converge a uniform start); the
+    plain FP64 kernel runs 20 + `plain_active` generations of the same slab
+    and seeds, and the two k are compared over the same generations."""
+    from nraps_gb300 import parity, synth
     prob = synth.scale_stress(seed)
-    d = measure_device(prob, "event", prob.generations - prob.skip, prob.skip, seed, device)
+    active = prob.generations - prob.skip
+    d = measure_device(prob, "event", active, prob.skip, seed, device, extra=dict(initial_source=1))
     per_launch_ms = d["transport_ms"] / max(1, d["transport_launches"])
     coll_per_launch = d["collisions"] / max(1, d["transport_launches"])
-    # the same run started from the deterministic diffusion fission source
-    dd = measure_device(prob, "event", prob.generations - prob.skip, prob.skip, seed, device,
-                        extra=dict(initial_source=1))
+    pp = prob.with_(generations=prob.skip + plain_active)
+    dp = measure_device(pp, "plain", plain_active, prob.skip, seed, device, extra=dict(initial_source=1))
+    # the same run from the reference's uniform fuel source, for comparison
+    du = measure_device(prob, "event", active, prob.skip, seed, device)
+    ke = d["k64"][prob.skip: prob.skip + plain_active]
+    kp = dp["k64"][prob.skip: prob.skip + plain_active]
+    me, se, _ = parity.batch_means(ke, 4)
+    mp, sp, _ = parity.batch_means(kp, 4)
+    sig = float(np.hypot(se, sp))
     return {"workload": "scale_stress", "cells": prob.n_cells, "regions": 10000, "groups": 8,
-            "diffusion_source": {"k_mean": dd["k_mean"], "sigma_k_pcm": dd["k_sigma"] * 1e5,
-                                 "histories_per_s": dd["histories"] / (dd["ms"] / 1000.0),
-                                 "collisions_per_s": dd["collisions"] / (dd["ms"] / 1000.0),
-                                 "collisions_per_history": dd["collisions"] / max(1, dd["histories"])},
-            "collisions_per_history": d["collisions"] / max(1, d["histories"]),
-            "histories_per_step": prob.histories, "steps": prob.generations - prob.skip,
+            "k_deterministic": prob.k_deterministic, "initial_source": "diffusion",
+            "histories_per_step": prob.histories, "steps": active,
             "histories_per_s": d["histories"] / (d["ms"] / 1000.0),
             "collisions_per_s": d["collisions"] / (d["ms"] / 1000.0),
-            "ms_per_step": d["ms"] / (prob.generations - prob.skip),
-            "sigma_k_pcm": d["k_sigma"] * 1e5, "k_mean": d["k_mean"],
+            "collisions_per_history": d["collisions"] / max(1, d["histories"]),
+            "ms_per_step": d["ms"] / active, "k_mean": d["k_mean"], "sigma_k_pcm": d["k_sigma"] * 1e5,
             "achieved_GBs": ALG_BYTES_PER_COLLISION * coll_per_launch / (per_launch_ms / 1000.0) / 1e9
-            if per_launch_ms > 0 else 0.0, "launch_shape": d["tuning"]}
+            if per_launch_ms > 0 else 0.0, "launch_shape": d["tuning"],
+            "plain_fp64": {"generations": f"{prob.skip} + {plain_active}",
+                           "histories_per_s": dp["histories"] / (dp["ms"] / 1000.0),
+                           "collisions_per_s": dp["collisions"] / (dp["ms"] / 1000.0),
+                           "ms_per_step": dp["ms"] / plain_active, "k_mean": dp["k_mean"],
+                           "sigma_k_pcm": dp["k_sigma"] * 1e5},
+            "event_vs_plain": {"generations": f"active {prob.skip}..{prob.skip + plain_active - 1} of both",
+                               "k_event": me, "k_plain": mp, "delta_k_pcm": (me - mp) * 1e5,
+                               "sigma_pcm": sig * 1e5, "z": (me - mp) / sig if sig > 0 else None,
+                               "sigma_from": "batch means, 4 batches of 5 generations"},
+            "uniform_source": {"k_mean": du["k_mean"], "sigma_k_pcm": du["k_sigma"] * 1e5,
+                               "histories_per_s": du["histories"] / (du["ms"] / 1000.0)}}
 
 
 def cpu_reference_rate(prob, budget_s: float, threads: int):
