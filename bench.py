@@ -170,7 +170,7 @@ ARMS = {
 }
 
 
-def measure_device(prob, arm: str, steps: int, warmup: int, seed: int, device: int, shape=None, pool=0,
+def measure_device(prob, arm: str, steps: int, warmup: int, seed: int, device: int, shape=None, sort=0,
                    extra=None):
     """Device-resident throughput: per-step CUDA events on the engine stream.
     shape = (block, events_per_pass, passes[, tail_lanes]) fixes the event launch shape
@@ -182,8 +182,8 @@ def measure_device(prob, arm: str, steps: int, warmup: int, seed: int, device: i
         kw.update(block_size=shape[0], events_per_pass=shape[1], passes=shape[2])
         if len(shape) > 3:
             kw.update(tail_lanes=shape[3])
-    if pool:
-        kw.update(pool_slots=pool)
+    if sort:
+        kw.update(sort_rounds=sort)
     if extra:
         kw.update(extra)
     ctx = api.Context(seed=seed, device=device, **kw)
@@ -478,7 +478,7 @@ def main():
     ap.add_argument("--serve-rate", type=float, default=200.0)
     ap.add_argument("--shape", type=lambda v: tuple(int(x) for x in v.split(",")), default=None,
                     help="block,events_per_pass,passes[,tail_lanes]: fixed event launch shape (profiling)")
-    ap.add_argument("--pool", type=int, default=0, help="pool transport with this many slots per block (profiling)")
+    ap.add_argument("--sort", type=int, default=0, help="sorted transport with this many rounds (profiling)")
     ap.add_argument("--initial-source", type=int, default=0, help="1 = start from the diffusion fission source")
     ap.add_argument("--range", type=int, default=0, help="ranged launches of this many histories (profiling)")
     ap.add_argument("--scale-stress", type=int, default=1, help="1 = also run the 10M-history, 200k-cell slab")
@@ -515,7 +515,7 @@ def main():
         extra["initial_source"] = args.initial_source
     if args.range:
         extra["range_len"] = args.range
-    d = measure_device(prob, arm, args.steps, args.warmup, seed, local, shape=args.shape, pool=args.pool,
+    d = measure_device(prob, arm, args.steps, args.warmup, seed, local, shape=args.shape, sort=args.sort,
                        extra=extra or None)
     clk = clocks.stop()
     ms = max_over_ranks(d["ms"], f"cuda:{local}")

@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define NRAPS_ABI_VERSION 5u
+#define NRAPS_ABI_VERSION 6u
 
 /* ---- status codes ------------------------------------------------------- */
 #define NRAPS_OK              0
@@ -98,11 +98,12 @@ typedef struct nraps_opts {
                                     warp with fewer live particles re-queues
                                     them for the next pass (needs passes >= 1);
                                     0 = off                                   */
-    uint32_t pool_slots;         /* WOODCOCK, one instance: > 0 = the pool
-                                    transport (particles kept in shared memory,
-                                    advanced in block-wide phases over
-                                    compacted lists) with this many slots per
-                                    block, 64..4096; 0 = tuned                */
+    uint32_t sort_rounds;        /* WOODCOCK, one instance: 1..16 = the sorted
+                                    transport (particles in event-type queues
+                                    in HBM: this many rounds of one flight
+                                    kernel and one collision kernel, then one
+                                    pass runs the survivors to their ends);
+                                    0 = tuned                                 */
     uint32_t initial_source;     /* BANK: 0 = the reference's uniform fuel source
                                     for generation 0; 1 = N sites drawn
                                     (deterministically) from the fission source
@@ -260,10 +261,14 @@ int  nraps_session_timing(nraps_session* s, double* transport_ms, double* total_
    events_per_pass and passes all 0 in the options, the first inactive
    generations each try one candidate shape (synchronously) and the one with
    the least time per real collision is kept; results do not depend on the
-   shape.  tried_ms receives the whole-generation time of each candidate
-   tried (up to tried_cap). */
+   shape.  The context remembers the choice per problem shape (MatTypes,
+   EnergyGroups, cells, Histories, mode, exact_log): a later session of the
+   same shape on the same context starts with it and tries nothing
+   (n_tried = 0), so repeated nraps_monte_carlo calls tune once.  tried_ms
+   receives the whole-generation time of each candidate tried (up to
+   tried_cap). */
 int  nraps_session_tuning(nraps_session* s, uint32_t* block, uint32_t* events_per_pass,
-                          uint32_t* passes, uint32_t* tail_lanes, uint32_t* pool_slots, uint32_t* range_len,
+                          uint32_t* passes, uint32_t* tail_lanes, uint32_t* sort_rounds, uint32_t* range_len,
                           uint32_t* n_tried, float* tried_ms, uint32_t tried_cap);
 /* generations completed so far (enqueued work included after sync) */
 uint64_t nraps_session_generation(const nraps_session* s);
@@ -342,6 +347,15 @@ int  nraps_batch_sync(nraps_batch* b);
 int  nraps_batch_results(nraps_batch* b, uint32_t i, nraps_result* out);
 /* device ms of all generations run, histories simulated, real collisions */
 int  nraps_batch_timing(nraps_batch* b, double* ms, uint64_t* histories, uint64_t* collisions);
+/* The batch's launch shape (a ranged pass: threads per block, histories per
+   range).  With block_size, range_len, events_per_pass and passes all 0 in
+   the options, the first inactive generations (as many as the smallest Skip
+   of the batch allows, at most 12) each try one of blocks of 128, 256 and
+   512 threads with ranges of 1024..8192 histories, synchronously, and the
+   shape with the least time per real collision is kept; every result is the
+   same whatever the shape.  tried_ms receives each tried generation's time. */
+int  nraps_batch_tuning(nraps_batch* b, uint32_t* block, uint32_t* range_len, uint32_t* n_tried,
+                        float* tried_ms, uint32_t tried_cap);
 uint32_t nraps_batch_size(const nraps_batch* b);
 void nraps_batch_destroy(nraps_batch* b);
 

@@ -12,7 +12,7 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-ABI_VERSION = 5
+ABI_VERSION = 6
 
 OK = 0
 ERR_INVALID = 1
@@ -50,7 +50,7 @@ class Opts(C.Structure):
         ("block_size", C.c_uint32), ("events_per_pass", C.c_uint32),
         ("passes", C.c_uint32), ("use_graphs", C.c_uint32),
         ("bank_factor", C.c_double), ("entropy_bins", C.c_uint32),
-        ("exact_log", C.c_uint32), ("tail_lanes", C.c_uint32), ("pool_slots", C.c_uint32),
+        ("exact_log", C.c_uint32), ("tail_lanes", C.c_uint32), ("sort_rounds", C.c_uint32),
         ("initial_source", C.c_uint32), ("range_len", C.c_uint32), ("reserved", C.c_uint32 * 2),
     ]
 
@@ -58,7 +58,7 @@ class Opts(C.Structure):
 def make_opts(*, seed=1, mode=MODE_COMPAT, precision=PREC_FP64, tracking=TRACK_SURFACE,
               compat_threads=0, max_events=0, block_size=0, events_per_pass=0, passes=0,
               use_graphs=0, bank_factor=0.0, entropy_bins=0, exact_log=0, device=-1, tail_lanes=0,
-              pool_slots=0, initial_source=0, range_len=0) -> Opts:
+              sort_rounds=0, initial_source=0, range_len=0) -> Opts:
     o = Opts()
     o.abi_version = ABI_VERSION
     o.device = device
@@ -76,7 +76,7 @@ def make_opts(*, seed=1, mode=MODE_COMPAT, precision=PREC_FP64, tracking=TRACK_S
     o.entropy_bins = entropy_bins
     o.exact_log = exact_log
     o.tail_lanes = tail_lanes
-    o.pool_slots = pool_slots
+    o.sort_rounds = sort_rounds
     o.initial_source = initial_source
     o.range_len = range_len
     return o

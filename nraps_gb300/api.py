@@ -89,6 +89,7 @@ def load(build_if_missing: bool = True):
     L.nraps_batch_sync.argtypes = [vp]
     L.nraps_batch_results.argtypes = [vp, C.c_uint32, P(abi.Result)]
     L.nraps_batch_timing.argtypes = [vp, P(C.c_double), P(C.c_uint64), P(C.c_uint64)]
+    L.nraps_batch_tuning.argtypes = [vp, P(C.c_uint32), P(C.c_uint32), P(C.c_uint32), P(C.c_float), C.c_uint32]
     L.nraps_batch_size.argtypes = [vp]
     L.nraps_batch_size.restype = C.c_uint32
     L.nraps_batch_destroy.argtypes = [vp]
@@ -426,7 +427,7 @@ class Session:
         _check(self._L.nraps_session_tuning(self.h, C.byref(b), C.byref(k), C.byref(pa), C.byref(t), C.byref(po),
                                             C.byref(rl), C.byref(n), ms, 32), self.ctx.h)
         return dict(block=b.value, events_per_pass=k.value, passes=pa.value, tail_lanes=t.value,
-                    pool_slots=po.value, range_len=rl.value, tried_ms=[ms[i] for i in range(min(n.value, 32))])
+                    sort_rounds=po.value, range_len=rl.value, tried_ms=[ms[i] for i in range(min(n.value, 32))])
 
     @property
     def generation(self) -> int:
@@ -509,6 +510,13 @@ class Batch:
         rv = res.view()
         _check(self._L.nraps_batch_results(self.h, i, C.byref(rv)), self.ctx.h)
         return res
+
+    def tuning(self) -> dict:
+        """Launch shape in use and the generation time of each tried shape."""
+        b, rl, n = C.c_uint32(), C.c_uint32(), C.c_uint32()
+        ms = (C.c_float * 32)()
+        _check(self._L.nraps_batch_tuning(self.h, C.byref(b), C.byref(rl), C.byref(n), ms, 32), self.ctx.h)
+        return dict(block=b.value, range_len=rl.value, tried_ms=[ms[i] for i in range(min(n.value, 32))])
 
     def timing(self) -> dict:
         ms, hist, coll = C.c_double(), C.c_uint64(), C.c_uint64()

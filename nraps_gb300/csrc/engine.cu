@@ -76,23 +76,39 @@ int validate_problem(nraps_ctx* ctx, const nraps_problem* p, const nraps_opts& o
     return NRAPS_OK;
 }
 
+cudaMemPool_t ctx_pool(nraps_ctx* ctx) {
+    if (ctx->pool) return ctx->pool;
+    cudaMemPoolProps props = {};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = ctx->device;
+    cudaMemPool_t p = nullptr;
+    if (cudaMemPoolCreate(&p, &props) != cudaSuccess) return nullptr;
+    /* keep freed memory in the pool: admissions after retirements reuse it */
+    uint64_t keep = ~0ULL;
+    cudaMemPoolSetAttribute(p, cudaMemPoolAttrReleaseThreshold, &keep);
+    ctx->pool = p;
+    return p;
+}
+
 cudaError_t InstBuffers::alloc(uint64_t G_, uint64_t nc_, uint64_t gens_, uint64_t N, double bank_factor, bool bank,
-                               double k0, GenState* st_ext, cudaStream_t s) {
+                               double k0, GenState* st_ext, cudaStream_t s, cudaMemPool_t pool) {
     G = G_; nc = nc_; gens = gens_;
     double bf = bank_factor > 0 ? bank_factor : 3.0;
     cap = bank ? (uint64_t)(bf * (double)N) + 1024 : 0;
     uint64_t nb = G * nc;
     cudaError_t e = cudaSuccess;
     auto A = [&](cudaError_t x) { if (e == cudaSuccess) e = x; };
-    A(tally.alloc(nb * 8)); A(flux_acc.alloc(nb * 8)); A(flux_sum.alloc(nb * 8)); A(flux_sq.alloc(nb * 8));
-    A(fs_acc.alloc(nc * 8)); A(k64.alloc(gens * 8)); A(entropy.alloc(gens * 8));
+    A(tally.alloc(nb * 8, pool, s)); A(flux_acc.alloc(nb * 8, pool, s)); A(flux_sum.alloc(nb * 8, pool, s));
+    A(flux_sq.alloc(nb * 8, pool, s));
+    A(fs_acc.alloc(nc * 8, pool, s)); A(k64.alloc(gens * 8, pool, s)); A(entropy.alloc(gens * 8, pool, s));
     if (bank) {
-        A(bank0.alloc(cap * sizeof(nraps_site))); A(bank1.alloc(cap * sizeof(nraps_site)));
-        A(hist.alloc(ev_hist_words(nc) * 4));
+        A(bank0.alloc(cap * sizeof(nraps_site), pool, s)); A(bank1.alloc(cap * sizeof(nraps_site), pool, s));
+        A(hist.alloc(ev_hist_words(nc) * 4, pool, s));
         if (e == cudaSuccess) A(cudaMemsetAsync(hist.p, 0, ev_hist_words(nc) * 4, s));
     }
     if (st_ext) st = st_ext;
-    else { A(own_state.alloc(sizeof(GenState))); st = own_state.as<GenState>(); }
+    else { A(own_state.alloc(sizeof(GenState), pool, s)); st = own_state.as<GenState>(); }
     if (e != cudaSuccess) return e;
     A(cudaMemsetAsync(tally.p, 0, nb * 8, s)); A(cudaMemsetAsync(flux_acc.p, 0, nb * 8, s));
     A(cudaMemsetAsync(flux_sum.p, 0, nb * 8, s)); A(cudaMemsetAsync(flux_sq.p, 0, nb * 8, s));
@@ -102,9 +118,9 @@ cudaError_t InstBuffers::alloc(uint64_t G_, uint64_t nc_, uint64_t gens_, uint64
     std::memset(&g0, 0, sizeof g0);
     g0.k = k0;
     g0.inv_kf = (float)(1.0 / k0);
+    /* from pageable memory: the copy is staged before the call returns, so
+       g0 may go out of scope */
     A(cudaMemcpyAsync(st, &g0, sizeof g0, cudaMemcpyHostToDevice, s));
-    /* the host copy must outlive the async copy */
-    A(cudaStreamSynchronize(s));
     return e;
 }
 
@@ -228,6 +244,7 @@ struct nraps_session {
     unsigned long long tune_coll = 0;    /* collisions before the next candidate  */
     size_t tune_next = 0;
     bool tuned = false;
+    std::array<uint64_t, 6> tune_key{};  /* the context's cache entry it fills   */
     ~nraps_session() {
         if (gexec) cudaGraphExecDestroy(gexec);
         for (cudaEvent_t e : tev) cudaEventDestroy(e);
@@ -384,25 +401,32 @@ int create_session(nraps_ctx* ctx, const nraps_problem* p, bool with_records, nr
         est = s->ev->commit(sm, e2);
         if (est) return set_err(ctx, est, e2);
         /* tune block size, collisions per pass and pass count unless all given */
+        const std::array<uint64_t, 6> key = {s->M, s->G, s->nc, s->N, (uint64_t)s->o.mode, (uint64_t)s->o.exact_log};
+        const auto hit = ctx->tuned.find(key);
         if (!with_records && s->o.block_size == 0 && s->o.events_per_pass == 0 && s->o.passes == 0 &&
-            s->o.tail_lanes == 0 && s->o.pool_slots == 0 && s->o.range_len == 0) {
-            /* {block, K, passes, tail, pool}; likeliest first: short
-               inactive phases try only the head.  The pool transport is
-               not a candidate: on the 1M-history slab it measured 60-75%
-               slower than the warp transport (fewer instructions per flight
-               did not make up for its block barriers and lower occupancy). */
+            s->o.tail_lanes == 0 && s->o.sort_rounds == 0 && s->o.range_len == 0 && hit != ctx->tuned.end()) {
+            /* tuned before on this context for a problem of this shape */
+            s->ev->params = hit->second;
+            int gs = s->ev->size_grid();
+            if (gs) return set_err(ctx, gs, "event engine: launch shape");
+            s->tuned = true;
+        } else if (!with_records && s->o.block_size == 0 && s->o.events_per_pass == 0 && s->o.passes == 0 &&
+            s->o.tail_lanes == 0 && s->o.sort_rounds == 0 && s->o.range_len == 0) {
+            s->tune_key = key;
+            /* likeliest first: short inactive phases try only the head.
+               {block, K, passes, tail, sort rounds, range} */
             const uint32_t X = NRAPS_ONE_PASS;
-            /* {block, K, passes, tail, pool, range} */
-            const uint32_t cand[][6] = {{256, X, 0, 0, 0, 0}, {128, X, 0, 0, 0, 1024}, {128, X, 0, 0, 0, 0},
-                                        {128, X, 0, 0, 0, 2048}, {256, X, 0, 0, 0, 2048}, {128, X, 0, 0, 0, 512},
-                                        {256, 16, 1, 0, 0, 0}, {256, X, 1, 12, 0, 0}, {256, 4, 1, 0, 0, 0},
-                                        {128, X, 0, 0, 0, 4096}};
+            const uint32_t cand[][6] = {{256, X, 0, 0, 0, 0}, {128, X, 0, 0, 0, 0}, {128, X, 0, 0, 8, 0},
+                                        {128, X, 0, 0, 0, 1024}, {128, X, 0, 0, 0, 4096},
+                                        {256, X, 0, 0, 0, 2048}, {128, X, 0, 0, 0, 2048}, {128, X, 0, 0, 12, 0},
+                                        {128, X, 0, 0, 0, 512}, {256, 16, 1, 0, 0, 0}, {256, X, 1, 12, 0, 0},
+                                        {256, 4, 1, 0, 0, 0}};
             size_t n = sizeof(cand) / sizeof(cand[0]);
             size_t budget = (size_t)std::min<uint64_t>(s->v.skip, n);
             for (size_t i = 0; i < budget; ++i) {
                 EvParams pr;
                 pr.block = cand[i][0]; pr.K = cand[i][1]; pr.passes = cand[i][2]; pr.tail = cand[i][3];
-                pr.pool = cand[i][4]; pr.range = cand[i][5];
+                pr.sort = cand[i][4]; pr.range = cand[i][5];
                 s->tune_cand.push_back(pr);
             }
             s->tuned = s->tune_cand.size() < 2;
@@ -504,6 +528,7 @@ void nraps_destroy(nraps_ctx* ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
     if (ctx->stream) { cudaStreamSynchronize(ctx->stream); cudaStreamDestroy(ctx->stream); }
+    if (ctx->pool) cudaMemPoolDestroy(ctx->pool);
     delete ctx;
 }
 
@@ -594,6 +619,7 @@ int nraps_session_run(nraps_session* s, uint64_t n) {
                 s->ev->params = s->tune_cand[best];
                 s->ev->size_grid();
                 s->tuned = true;
+                ctx->tuned[s->tune_key] = s->tune_cand[best];
             }
             s->enqueued++;
             continue;
@@ -662,7 +688,7 @@ int nraps_session_sync(nraps_session* s) {
 }
 
 int nraps_session_tuning(nraps_session* s, uint32_t* block, uint32_t* events_per_pass, uint32_t* passes,
-                         uint32_t* tail_lanes, uint32_t* pool_slots, uint32_t* range_len, uint32_t* n_tried,
+                         uint32_t* tail_lanes, uint32_t* sort_rounds, uint32_t* range_len, uint32_t* n_tried,
                          float* tried_ms, uint32_t tried_cap) {
     if (!s) return NRAPS_ERR_INVALID;
     if (!s->ev) return set_err(s->ctx, NRAPS_ERR_INVALID, "tuning applies to WOODCOCK sessions");
@@ -670,7 +696,7 @@ int nraps_session_tuning(nraps_session* s, uint32_t* block, uint32_t* events_per
     if (events_per_pass) *events_per_pass = s->ev->params.K;
     if (passes) *passes = s->ev->params.passes;
     if (tail_lanes) *tail_lanes = s->ev->params.tail;
-    if (pool_slots) *pool_slots = s->ev->params.pool;
+    if (sort_rounds) *sort_rounds = s->ev->params.sort;
     if (range_len) *range_len = s->ev->params.range;
     if (n_tried) *n_tried = (uint32_t)s->tune_ms.size();
     for (uint32_t i = 0; tried_ms && i < tried_cap && i < s->tune_ms.size(); ++i) tried_ms[i] = s->tune_ms[i];

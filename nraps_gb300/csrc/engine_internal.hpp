@@ -8,6 +8,8 @@
 
 #include <cuda_runtime.h>
 
+#include <array>
+#include <map>
 #include <string>
 
 #include "../../include/nraps_gpu.h"
@@ -21,6 +23,13 @@ struct nraps_ctx {
     cudaStream_t stream = nullptr;
     std::string err;
     uint64_t launches = 0;
+    /* launch shape the autotuner chose, per problem shape (materials,
+       groups, cells, histories, mode, log): a later session of the same
+       shape on this context starts with it instead of tuning again */
+    std::map<std::array<uint64_t, 6>, EvParams> tuned;
+    /* stream-ordered memory pool of this context's device (created on first
+       use, kept until the context is destroyed) */
+    cudaMemPool_t pool = nullptr;
 };
 
 namespace nrint {
@@ -34,17 +43,32 @@ inline int cuda_status(cudaError_t e) {
     return e == cudaErrorMemoryAllocation ? NRAPS_ERR_NOMEM : NRAPS_ERR_CUDA;
 }
 
+/* Device memory: cudaMalloc, or (alloc with a pool) stream-ordered from a
+   memory pool, which neither synchronises the device nor returns memory to
+   the driver, and is freed in the same stream's order. */
 struct DevMem {
     void* p = nullptr;
     size_t n = 0;
+    cudaStream_t fs = nullptr;          /* stream-ordered: the stream it is freed on */
+    bool pooled = false;
     DevMem() = default;
     DevMem(const DevMem&) = delete;
     DevMem& operator=(const DevMem&) = delete;
-    ~DevMem() { if (p) cudaFree(p); }
-    cudaError_t alloc(size_t bytes) {
-        if (p) { cudaFree(p); p = nullptr; }
+    ~DevMem() { release(); }
+    void release() {
+        if (p) { if (pooled) cudaFreeAsync(p, fs); else cudaFree(p); }
+        p = nullptr;
+        pooled = false;
+    }
+    cudaError_t alloc(size_t bytes, cudaMemPool_t pool = nullptr, cudaStream_t s = nullptr) {
+        release();
         n = bytes;
         if (bytes == 0) return cudaSuccess;
+        if (pool) {
+            pooled = true;
+            fs = s;
+            return cudaMallocFromPoolAsync(&p, bytes, pool, s);
+        }
         return cudaMalloc(&p, bytes);
     }
     template <class T> T* as() const { return reinterpret_cast<T*>(p); }
@@ -55,9 +79,12 @@ struct InstBuffers {
     DevMem tally, flux_acc, flux_sum, flux_sq, fs_acc, k64, entropy, bank0, bank1, hist, own_state;
     GenState* st = nullptr;
     uint64_t G = 0, nc = 0, gens = 0, cap = 0;
-    /* st_ext: a GenState slot owned by the caller, or nullptr to own one */
+    /* st_ext: a GenState slot owned by the caller, or nullptr to own one;
+       pool: allocate stream-ordered on s from this pool (no device-wide
+       synchronisation: the request server admits and retires many
+       instances), or nullptr for cudaMalloc */
     cudaError_t alloc(uint64_t G_, uint64_t nc_, uint64_t gens_, uint64_t N, double bank_factor, bool bank,
-                      double k0, GenState* st_ext, cudaStream_t s);
+                      double k0, GenState* st_ext, cudaStream_t s, cudaMemPool_t pool = nullptr);
     EvBuffers view(uint64_t skip, uint64_t seed) const;
     uint64_t bytes() const;
 };
@@ -70,6 +97,9 @@ struct ResultsView {
     double transport_ms, total_ms;
     uint64_t transport_launches, gpu_launches;
 };
+
+/* The context's memory pool (created on first call; nullptr on failure). */
+cudaMemPool_t ctx_pool(nraps_ctx* ctx);
 
 /* Copies device results into `out` (synchronous on the current device). */
 int fetch_results(nraps_ctx* ctx, const ResultsView& v, nraps_result* out);

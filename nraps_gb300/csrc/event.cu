@@ -82,15 +82,12 @@ struct EvInst {
     const float* xs;          /* [(m*G+g)*4]: sigtr, pabs, nsf_st, inv_st      */
     const double* inv_st64;   /* [m*G+g] flux score                            */
     const unsigned long long* kq; /* [m*G+g] k score in 2^-32 fixed point      */
-    const float* scdf;        /* [(m*G+g)*G + e]                               */
+    const float* ocdf;        /* [(m*G+g)*G + e] outcome CDF of a collision    */
     const float* chicdf;      /* [m*G + g]                                     */
     const float* maj;         /* [g] majorant, [G+g] inverse                   */
-    const float* rleft;       /* R+1                                           */
-    const float* rinvdx;      /* R                                             */
+    const float4* rdat;       /* R+1: left edge, 1/dx, first cell, cells       */
     const uint8_t* rmat;      /* R                                             */
-    const uint32_t* rfirst;   /* R                                             */
-    const uint32_t* rncell;   /* R                                             */
-    const uint16_t* grid;     /* nbins                                         */
+    const uint2* bins;        /* nbins: next boundary, first region | multi<<31 */
     const uint32_t* fuel;     /* nfuel                                         */
     const float* cleft;       /* nc                                            */
     const float* cdx;         /* nc                                            */
@@ -160,6 +157,16 @@ struct EvArgs {
     uint32_t* rb_fill;               /* ranges: sites the range appended        */
     unsigned long long* rb_base;     /* ranges: first bank position in its instance */
     unsigned long long* rb_total;    /* n_inst: sites of the generation         */
+    /* sorted transport: the collision queue (structure of arrays, the
+       flight queue's record plus the region of the collision) and its fill
+       per round */
+    float* cx;
+    float* cmu;
+    unsigned long long* crng;
+    uint32_t* cid;
+    uint32_t* cpk;
+    uint32_t* creg;
+    unsigned long long* ccount;      /* MAX_PASSES+2                            */
 };
 
 /* ranged bank geometry */
@@ -176,18 +183,15 @@ constexpr uint32_t RB_SPIN_MAX = 1u << 20;   /* bound on waiting for a chunk id 
 
 /* table view: shared memory (single instance) or the instance's globals */
 struct TView {
-    const float* xs;
+    const float4* xs;             /* [m*G+g]: sigtr, pabs, nsf_st, inv_st     */
     const double* inv_st64;
     const unsigned long long* kq;
-    const float* scdf;
+    const float* ocdf;
     const float* chi;
     const float* maj;
-    const float* left;
-    const uint16_t* grid;
+    const float4* rdat;
+    const uint2* bins;
     const uint8_t* rmat;
-    const float* invdx;
-    const uint32_t* first;
-    const uint32_t* ncell;
     uint32_t G, R, nbins;
     float L, inv_binw, boundl, boundr;
 };
@@ -200,12 +204,17 @@ template <bool EXACT> __device__ __forceinline__ float neg_log(float u) {
     return -__logf(u);
 }
 
+/* region r with left[r] <= x < left[r+1] (the last region for x == L), for
+   0 <= x <= L: the bin gives the first region its points can lie in and the
+   next boundary; a bin with several boundaries walks on (bins are narrower
+   than half the narrowest region unless their count is capped) */
 __device__ __forceinline__ uint32_t region_of(const TView& t, float x) {
     int b = (int)__fmul_rn(x, t.inv_binw);
     b = b < 0 ? 0 : (b >= (int)t.nbins ? (int)t.nbins - 1 : b);
-    uint32_t r = t.grid[b];
-    while (r + 1 < t.R && x >= t.left[r + 1]) ++r;
-    while (r > 0 && x < t.left[r]) --r;
+    const uint2 e = t.bins[b];
+    uint32_t r = (e.y & 0x7FFFFFFFu) + (x >= __uint_as_float(e.x) ? 1u : 0u);
+    if (e.y & 0x80000000u)
+        while (r + 1 < t.R && x >= t.rdat[r + 1].x) ++r;
     return r;
 }
 
@@ -216,10 +225,11 @@ __device__ __forceinline__ uint32_t count_below(const float* cdf, uint32_t G, fl
     for (uint32_t e = 0; e < G; ++e) n += (cdf[e] < v) ? 1u : 0u;
     return n < G - 1 ? n : G - 1;
 }
-/* first e with v < cdf[e] (G-1 if none) == number of the first G-1 entries <= v */
-__device__ __forceinline__ uint32_t count_le(const float* cdf, uint32_t G, float v) {
+/* number of the G entries of a collision's outcome CDF that are <= v:
+   0 = absorbed, n >= 1 = scattered into group n - 1 */
+__device__ __forceinline__ uint32_t count_outcome(const float* cdf, uint32_t G, float v) {
     uint32_t n = 0;
-    for (uint32_t e = 0; e + 1 < G; ++e) n += (cdf[e] <= v) ? 1u : 0u;
+    for (uint32_t e = 0; e < G; ++e) n += (cdf[e] <= v) ? 1u : 0u;
     return n;
 }
 
@@ -285,58 +295,52 @@ __device__ __forceinline__ uint64_t bank_site(uint64_t i, uint64_t nbk, const ND
 
 __device__ __forceinline__ TView global_view(const EvInst& I) {
     TView t;
-    t.xs = I.xs; t.inv_st64 = I.inv_st64; t.kq = I.kq; t.scdf = I.scdf; t.chi = I.chicdf; t.maj = I.maj;
-    t.left = I.rleft; t.grid = I.grid; t.rmat = I.rmat; t.invdx = I.rinvdx; t.first = I.rfirst;
-    t.ncell = I.rncell;
+    t.xs = reinterpret_cast<const float4*>(I.xs); t.inv_st64 = I.inv_st64; t.kq = I.kq; t.ocdf = I.ocdf;
+    t.chi = I.chicdf; t.maj = I.maj; t.rdat = I.rdat; t.bins = I.bins; t.rmat = I.rmat;
     t.G = I.G; t.R = I.R; t.nbins = I.nbins; t.L = I.L; t.inv_binw = I.inv_binw;
     t.boundl = I.boundl; t.boundr = I.boundr;
     return t;
 }
 
-/* shared-memory footprint of one instance's tables */
+/* shared-memory footprint of one instance's tables: 8-byte and 16-byte
+   arrays first, then floats, then bytes */
 __host__ __device__ __forceinline__ size_t smem_bytes_for(uint32_t M, uint32_t G, uint32_t R, uint32_t nbins) {
-    size_t b = (size_t)M * G * 16;                          /* inv_st64 + kq      */
-    b += ((size_t)M * G * 4 + (size_t)M * G * G + (size_t)M * G + 2 * G + (R + 1) + 3 * (size_t)R) * 4;
-    b += (size_t)nbins * 2 + R;
+    const size_t MG = (size_t)M * G;
+    size_t b = MG * 16 + MG * 16 + ((size_t)R + 1) * 16 + (size_t)nbins * 8;
+    b += (MG * G + MG + 2 * (size_t)G) * 4 + R;
     return (b + 15) / 16 * 16;
 }
 
 /* Copies one instance's tables into shared memory at tab (block-wide; the
    caller synchronises) and points t at them. */
 __device__ __forceinline__ void stage_tables(const EvInst& I, unsigned char* tab, TView& t) {
-    const uint32_t M = I.M, G = I.G, R = I.R, NB = I.nbins;
+    const uint32_t M = I.M, G = I.G, R = I.R, NB = I.nbins, MG = M * G;
     double* s_inv64 = reinterpret_cast<double*>(tab);
-    unsigned long long* s_kq = reinterpret_cast<unsigned long long*>(s_inv64 + M * G);
-    float* f = reinterpret_cast<float*>(s_kq + M * G);
-    float* s_xs = f;                 f += M * G * 4;
-    float* s_scdf = f;               f += M * G * G;
-    float* s_chi = f;                f += M * G;
-    float* s_maj = f;                f += 2 * G;
-    float* s_left = f;               f += R + 1;
-    float* s_invdx = f;              f += R;
-    uint32_t* s_first = reinterpret_cast<uint32_t*>(f);  f += R;
-    uint32_t* s_ncell = reinterpret_cast<uint32_t*>(f);  f += R;
-    uint16_t* s_grid = reinterpret_cast<uint16_t*>(f);
-    uint8_t* s_rmat = reinterpret_cast<uint8_t*>(s_grid + NB);
-    for (uint32_t i = threadIdx.x; i < M * G; i += blockDim.x) { s_inv64[i] = I.inv_st64[i]; s_kq[i] = I.kq[i]; }
-    for (uint32_t i = threadIdx.x; i < M * G * 4; i += blockDim.x) s_xs[i] = I.xs[i];
-    for (uint32_t i = threadIdx.x; i < M * G * G; i += blockDim.x) s_scdf[i] = I.scdf[i];
-    for (uint32_t i = threadIdx.x; i < M * G; i += blockDim.x) s_chi[i] = I.chicdf[i];
-    for (uint32_t i = threadIdx.x; i < 2 * G; i += blockDim.x) s_maj[i] = I.maj[i];
-    for (uint32_t i = threadIdx.x; i < R + 1; i += blockDim.x) s_left[i] = I.rleft[i];
-    for (uint32_t i = threadIdx.x; i < R; i += blockDim.x) {
-        s_invdx[i] = I.rinvdx[i]; s_first[i] = I.rfirst[i]; s_ncell[i] = I.rncell[i];
+    unsigned long long* s_kq = reinterpret_cast<unsigned long long*>(s_inv64 + MG);
+    float4* s_xs = reinterpret_cast<float4*>(s_kq + MG);
+    float4* s_rdat = s_xs + MG;
+    uint2* s_bins = reinterpret_cast<uint2*>(s_rdat + R + 1);
+    float* s_ocdf = reinterpret_cast<float*>(s_bins + NB);
+    float* s_chi = s_ocdf + MG * G;
+    float* s_maj = s_chi + MG;
+    uint8_t* s_rmat = reinterpret_cast<uint8_t*>(s_maj + 2 * G);
+    const float4* g_xs = reinterpret_cast<const float4*>(I.xs);
+    for (uint32_t i = threadIdx.x; i < MG; i += blockDim.x) {
+        s_inv64[i] = I.inv_st64[i]; s_kq[i] = I.kq[i]; s_xs[i] = g_xs[i];
     }
-    for (uint32_t i = threadIdx.x; i < NB; i += blockDim.x) s_grid[i] = I.grid[i];
+    for (uint32_t i = threadIdx.x; i <= R; i += blockDim.x) s_rdat[i] = I.rdat[i];
+    for (uint32_t i = threadIdx.x; i < NB; i += blockDim.x) s_bins[i] = I.bins[i];
+    for (uint32_t i = threadIdx.x; i < MG * G; i += blockDim.x) s_ocdf[i] = I.ocdf[i];
+    for (uint32_t i = threadIdx.x; i < MG; i += blockDim.x) s_chi[i] = I.chicdf[i];
+    for (uint32_t i = threadIdx.x; i < 2 * G; i += blockDim.x) s_maj[i] = I.maj[i];
     for (uint32_t i = threadIdx.x; i < R; i += blockDim.x) s_rmat[i] = I.rmat[i];
-    t.xs = s_xs; t.inv_st64 = s_inv64; t.kq = s_kq; t.scdf = s_scdf; t.chi = s_chi; t.maj = s_maj;
-    t.left = s_left; t.grid = s_grid; t.rmat = s_rmat; t.invdx = s_invdx; t.first = s_first;
-    t.ncell = s_ncell;
+    t.xs = s_xs; t.inv_st64 = s_inv64; t.kq = s_kq; t.ocdf = s_ocdf; t.chi = s_chi; t.maj = s_maj;
+    t.rdat = s_rdat; t.bins = s_bins; t.rmat = s_rmat;
     t.G = G; t.R = R; t.nbins = NB; t.L = I.L; t.inv_binw = I.inv_binw;
     t.boundl = I.boundl; t.boundr = I.boundr;
 }
 
-constexpr int WARPS_MAX = 8;        /* blocks of at most 256 threads          */
+constexpr int WARPS_MAX = 8;        /* batched (ONE = 0) blocks: at most 256 threads */
 struct Stage;
 __host__ __device__ __forceinline__ size_t stage_bytes(uint32_t block);
 constexpr uint32_t CHUNK = 64;      /* particles a warp claims per atomic     */
@@ -444,12 +448,15 @@ __device__ __forceinline__ void move_down(Stage& sg, uint32_t from, uint32_t n, 
  * lanes, fly every live lane once per iteration, process real collisions,
  * stage fission sites and particles that completed K real collisions.
  */
-template <bool SOURCE, int ONE, bool EXACT, bool BANK, bool REC>
+template <bool SOURCE, int ONE, bool EXACT, bool BANK, bool REC, bool OP>
 __device__ __forceinline__ void ev_pass_body(const EvArgs& a, int pass, uint32_t K, uint32_t tail) {
     /* ONE: 0 batched (instances mixed in a warp), 1 one instance, 2 ranged
        (block b runs range b of one instance, that instance's tables staged
        in shared memory), 3 ranged with the tables read from global memory
-       (instances whose tables do not fit) */
+       (instances whose tables do not fit).  OP: one pass (every particle
+       runs to its end; no survivor queue, no tail hand-off) -- K and tail
+       are then ignored. */
+    static_assert(!OP || SOURCE, "a one-pass launch starts from the source");
     constexpr bool RANGED = ONE >= 2;
     constexpr bool SMEM_TAB = ONE == 1 || ONE == 2;
     nrdev::pdl_trigger();
@@ -537,7 +544,8 @@ __device__ __forceinline__ void ev_pass_body(const EvArgs& a, int pass, uint32_t
     bool have = false;
     Part p;
     uint32_t done = 0;
-    uint64_t events = 0;
+    uint32_t events = 0;
+    const uint32_t max_ev = a.max_events < 0xFFFFFFFFull ? (uint32_t)a.max_events : 0xFFFFFFFFu;
     const EvInst* Ip = &a.inst[inst0];
     TView tv = t;
     uint32_t tv_inst = 0xFFFFFFFFu;          /* batched: instance tv describes  */
@@ -597,13 +605,13 @@ __device__ __forceinline__ void ev_pass_body(const EvArgs& a, int pass, uint32_t
                             const uint32_t local = (uint32_t)(idx - hb);
                             nr_pcg32 rng = nr_pcg32_seeded(gseed, local);
                             float bx = 0.0f, bmu;
-                            uint32_t bg = 0;
+                            uint32_t bg = 0, bcell = 0;
                             bool banked = false;
                             if (BANK && ONE) {
                                 if (s_src.nbk > 0) {
-                                    /* one 16-byte load of the site (x, cell, group, pad) */
+                                    /* one 16-byte load of the site (x, cell, -, -) */
                                     const uint4 sv = reinterpret_cast<const uint4*>(s_src.bank)[bank_site(local, s_src.nbk, s_src.ndiv)];
-                                    bx = __uint_as_float(sv.x); bg = sv.z; banked = true;
+                                    bx = __uint_as_float(sv.x); bcell = sv.y; banked = true;
                                 }
                             } else if (BANK) {
                                 const GenState* st = I.st;
@@ -611,11 +619,15 @@ __device__ __forceinline__ void ev_pass_body(const EvArgs& a, int pass, uint32_t
                                 if (nbk > 0) {
                                     const nraps_site* bank = I.bank[st->gen & 1];
                                     const uint4 sv = reinterpret_cast<const uint4*>(bank)[bank_site(local, nbk, I.ndiv)];
-                                    bx = __uint_as_float(sv.x); bg = sv.z; banked = true;
+                                    bx = __uint_as_float(sv.x); bcell = sv.y; banked = true;
                                 }
                             }
                             if (banked) {
+                                /* a fission neutron's group is drawn at its birth, from chi
+                                   of the material it was born in */
                                 bmu = __fsub_rn(__fmul_rn(2.0f, u24(nr_pcg32_next(&rng))), 1.0f);
+                                const uint32_t c = bcell < I.nc ? bcell : I.nc - 1;
+                                bg = count_below(I.chicdf + (uint32_t)I.cmat[c] * I.G, I.G, u24(nr_pcg32_next(&rng)));
                             } else {
                                 /* fresh uniform fuel source (spawn_neutron) */
                                 const uint32_t cell = I.fuel[((uint64_t)nr_pcg32_next(&rng) * I.nfuel) >> 32];
@@ -624,7 +636,7 @@ __device__ __forceinline__ void ev_pass_body(const EvArgs& a, int pass, uint32_t
                                 bmu = __fsub_rn(__fmul_rn(2.0f, u24(nr_pcg32_next(&rng))), 1.0f);
                                 bg = count_below(I.chicdf + (uint32_t)I.cmat[cell] * I.G, I.G, u24(nr_pcg32_next(&rng)));
                             }
-                            if (REC && inst == 0) a.rec[local].draws += banked ? 1 : 4;
+                            if (REC && inst == 0) a.rec[local].draws += banked ? 2 : 4;
                             sg.pf_a[k] = make_uint4(__float_as_uint(bx), __float_as_uint(bmu), (uint32_t)idx,
                                                     bg | (inst << 4));
                             sg.pf_rng[k] = rng.state;
@@ -681,7 +693,7 @@ __device__ __forceinline__ void ev_pass_body(const EvArgs& a, int pass, uint32_t
         /* ---- tail hand-off: input used up and few lanes still live -------
            every live particle goes to the next pass's queue (at the start of
            its next flight, so its history is unchanged) and the warp leaves */
-        if (tail && exhausted) {
+        if (!OP && tail && exhausted) {
             const unsigned live = __ballot_sync(FULL, have);
             if ((uint32_t)__popc(live) < tail) {
                 if (have) {
@@ -715,7 +727,7 @@ __device__ __forceinline__ void ev_pass_body(const EvArgs& a, int pass, uint32_t
                so the next flight runs converged with the other lanes' flights
                (looping over virtual collisions here measured 30% more
                instructions: the extra iterations run divergent) */
-            if (++events > a.max_events) {
+            if (++events > max_ev) {
                 fate = NRAPS_FATE_CAPPED;
             } else {
                 float d = __fmul_rn(neg_log<EXACT>(u24pos(next())), tv.maj[G + p.g]);
@@ -734,15 +746,17 @@ __device__ __forceinline__ void ev_pass_body(const EvArgs& a, int pass, uint32_t
                 if (fate < 0) {
                     uint32_t r = region_of(tv, p.x);
                     m = tv.rmat[r];
-                    if (__fmul_rn(u24(next()), tv.maj[p.g]) < tv.xs[(m * G + p.g) * 4]) {
+                    const uint32_t j = m * G + p.g;
+                    const float4 X = tv.xs[j];
+                    if (__fmul_rn(u24(next()), tv.maj[p.g]) < X.x) {
                         real = true;
                         acc.coll++;
-                        float rel = __fmul_rn(__fsub_rn(p.x, tv.left[r]), tv.invdx[r]);
-                        uint32_t nr = tv.ncell[r];
+                        const float4 rd = tv.rdat[r];
+                        float rel = __fmul_rn(__fsub_rn(p.x, rd.x), rd.y);
+                        const uint32_t nr = __float_as_uint(rd.w);
                         uint32_t k = rel > 0.0f ? (uint32_t)rel : 0u;
                         if (k >= nr) k = nr - 1;
-                        cell = tv.first[r] + k;
-                        const uint32_t j = m * G + p.g;
+                        cell = __float_as_uint(rd.z) + k;
                         {
                             const Hot& h = s_hot[ONE ? 0 : threadIdx.x];
                             nrdev::red_add_f64(&h.tally[(uint64_t)p.g * h.nc + cell], tv.inv_st64[j]);
@@ -753,11 +767,11 @@ __device__ __forceinline__ void ev_pass_body(const EvArgs& a, int pass, uint32_t
                         if (REC && rec) {
                             rec->collisions++;
                             rec->track += tv.inv_st64[j];
-                            rec->nsf_track += (double)tv.xs[j * 4 + 2];
+                            rec->nsf_track += (double)X.z;
                             rec->final_cell = cell;
                         }
                         if (BANK) {
-                            float nu = __fadd_rn(__fmul_rn(tv.xs[j * 4 + 2], inv_k), u24(next()));
+                            float nu = __fadd_rn(__fmul_rn(X.z, inv_k), u24(next()));
                             int n = (int)floorf(nu);
                             pending = n > 64 ? 64u : (uint32_t)n;
                         }
@@ -768,14 +782,14 @@ __device__ __forceinline__ void ev_pass_body(const EvArgs& a, int pass, uint32_t
                 }
             }
         }
-        /* ---- fission sites: one per pending lane per round ------------------ */
+        /* ---- fission sites: one per pending lane per round ------------------
+           a site is a position and a cell; the child draws its group at birth */
         if (BANK) {
             while (__any_sync(FULL, pending > 0)) {
                 unsigned sm = __ballot_sync(FULL, pending > 0);
                 if (pending > 0) {
-                    uint32_t sgp = count_below(tv.chi + m * G, G, u24(next()));
                     uint32_t slot = staged_sites + __popc(sm & lt);
-                    sg.site[slot] = make_uint4(__float_as_uint(p.x), cell | (sgp << 27), p.id,
+                    sg.site[slot] = make_uint4(__float_as_uint(p.x), cell, p.id,
                                                (p.seq & 0xFFFFu) | (p.inst << 16));
                     if (p.seq >= 0xFFFFu) atomicOr(&Ip->st->error, NR_ERR_CAPACITY);
                     p.seq++;
@@ -796,14 +810,16 @@ __device__ __forceinline__ void ev_pass_body(const EvArgs& a, int pass, uint32_t
         bool push = false;
         if (have) {
             if (real) {
+                /* one uniform decides absorption and the scatter group */
                 const uint32_t j = m * G + p.g;
-                if (u24(next()) < tv.xs[j * 4 + 1]) {
+                const uint32_t o = count_outcome(tv.ocdf + j * G, G, u24(next()));
+                if (o == 0) {
                     fate = NRAPS_FATE_ABSORBED;
                 } else {
-                    p.g = count_le(tv.scdf + j * G, G, u24(next()));
+                    p.g = o - 1;
                     p.mu = __fsub_rn(__fmul_rn(2.0f, u24(next())), 1.0f);
                 }
-                ++done;
+                if (!OP) ++done;
             }
             if (REC && rec) rec->draws += draws;
             if (fate >= 0) {
@@ -816,14 +832,14 @@ __device__ __forceinline__ void ev_pass_body(const EvArgs& a, int pass, uint32_t
                     rec->n_sites = p.seq;
                 }
                 have = false;
-            } else if (real && done >= K) {
+            } else if (!OP && real && done >= K) {
                 push = true;
                 have = false;
             }
         }
         /* ---- stage survivors; flush 32 at a time ------------------------------ */
-        unsigned pm = __ballot_sync(FULL, push);
-        if (pm) {
+        const unsigned pm = OP ? 0u : __ballot_sync(FULL, push);
+        if (!OP && pm) {
             if (push) {
                 uint32_t slot = staged + __popc(pm & lt);
                 sg.x[slot] = p.x; sg.mu[slot] = p.mu; sg.rng[slot] = p.rng.state;
@@ -873,328 +889,278 @@ __device__ __forceinline__ void ev_pass_body(const EvArgs& a, int pass, uint32_t
    1-2% faster on single_large), 64 for ranged launches with the tables in
    shared memory, 80 where table pointers are global (batched, ranged over
    large tables). */
-template <bool SOURCE, int ONE, bool EXACT, bool BANK, bool REC>
+template <bool SOURCE, int ONE, bool EXACT, bool BANK, bool REC, bool OP>
 __global__ void __launch_bounds__(256, ONE == 2 ? 4 : 3) ev_pass(EvArgs a, int pass, uint32_t K, uint32_t tail) {
-    ev_pass_body<SOURCE, ONE, EXACT, BANK, REC>(a, pass, K, tail);
+    ev_pass_body<SOURCE, ONE, EXACT, BANK, REC, OP>(a, pass, K, tail);
 }
-template <bool SOURCE, bool EXACT, bool BANK, bool REC>
+template <bool SOURCE, bool EXACT, bool BANK, bool REC, bool OP>
 __global__ void __maxnreg__(56) ev_pass_one(EvArgs a, int pass, uint32_t K, uint32_t tail) {
-    ev_pass_body<SOURCE, 1, EXACT, BANK, REC>(a, pass, K, tail);
+    ev_pass_body<SOURCE, 1, EXACT, BANK, REC, OP>(a, pass, K, tail);
+}
+/* ranged launches in 512-thread blocks (an autotuner candidate for batches:
+   fewer, larger blocks stage each range's tables once for twice the warps) */
+template <int ONE, bool EXACT, bool BANK>
+__global__ void __launch_bounds__(512, 2) ev_pass_wide(EvArgs a, int pass, uint32_t K, uint32_t tail) {
+    static_assert(ONE >= 2, "512-thread blocks run ranged launches");
+    ev_pass_body<true, ONE, EXACT, BANK, false, true>(a, pass, K, tail);
 }
 /* the kernel of one instantiation */
-template <bool SOURCE, int ONE, bool EXACT, bool BANK, bool REC>
+template <bool SOURCE, int ONE, bool EXACT, bool BANK, bool REC, bool OP>
 constexpr auto pass_kernel() {
-    if constexpr (ONE == 1) return &ev_pass_one<SOURCE, EXACT, BANK, REC>;
-    else return &ev_pass<SOURCE, ONE, EXACT, BANK, REC>;
+    if constexpr (ONE == 1) return &ev_pass_one<SOURCE, EXACT, BANK, REC, OP>;
+    else return &ev_pass<SOURCE, ONE, EXACT, BANK, REC, OP>;
 }
 
 /*
- * Pool transport (single instance, tables in shared memory, one pass: every
- * particle runs to its end).  Each block keeps up to P particles in shared
- * memory as structure-of-arrays and advances them in block-wide phases over
- * compacted slot lists, so the threads of a phase run the same code:
- *   refill  births into the free slots (one claim per block per round);
- *   A       one flight per live particle: distance, boundary, region,
- *           Woodcock test -> real collisions to list R, virtual ones stay
- *           live, leaked and capped histories end;
- *   B       one real collision per particle of R: tally and k scores,
- *           fission sites, absorption (ends) or scatter (stays live).
- * In ev_pass a warp executes every path any of its lanes takes, each with
- * the lanes that take it; here a phase's threads share one path.  A
- * particle's draws are the same sequence as in ev_pass, so every history,
- * and every result, is the same as with any other launch shape.
+ * Sorted transport (one instance).  Particles wait in structure-of-arrays
+ * queues in HBM, and each event type runs in its own kernel over a queue
+ * that holds only that event, so the lanes of a warp run the same code:
+ *   ev_sort_flight   one flight per particle of round r's flight queue (in
+ *                    round 0, the births): a leak ends the history, a virtual
+ *                    collision puts the particle in round r+1's flight queue,
+ *                    a real collision in round r's collision queue (with the
+ *                    region it happened in);
+ *   ev_sort_collide  one real collision per particle of the collision queue:
+ *                    tally and k scores, fission sites, then absorption (the
+ *                    history ends) or scatter (round r+1's flight queue).
+ * Queue appends are warp-aggregated (one atomic per warp and queue).  After
+ * R rounds the surviving particles run to their ends in one pass of the warp
+ * transport (pass R, reading round R-1's output queue).  A particle draws the
+ * same numbers in the same order as in ev_pass, so every history -- and with
+ * it k, the tallies and the ordered bank -- is the same as with any other
+ * launch shape.  Tables are read through L1 (no staging: a round's kernels
+ * are short).
  */
-constexpr int POOL_THREADS = 256;
-constexpr int POOL_WARPS = POOL_THREADS / 32;
-constexpr uint32_t POOL_MAX = 4096;          /* slot indices are u16 */
-
-struct PoolSite {
+struct SiteStage {
     uint4 site[STAGE];
 };
+constexpr size_t SORT_STAGE_BYTES = (256 / 32) * sizeof(SiteStage);   /* 256-thread blocks */
 
-/* shared memory of the pool (slots, lists, site staging), before the tables */
-__host__ __device__ __forceinline__ size_t pool_bytes(uint32_t P) {
-    size_t b = (size_t)P * (8 + 4 * 6) + (size_t)P * 2 * 4;
-    b = (b + 15) & ~(size_t)15;
-    return b + POOL_WARPS * sizeof(PoolSite);
+/* sites [from, from+n) of a warp's staging -> [0, n), n <= 32 */
+__device__ __forceinline__ void move_sites_down(SiteStage& sg, uint32_t from, uint32_t n, uint32_t lane) {
+    uint4 v = make_uint4(0, 0, 0, 0);
+    if (lane < n) v = sg.site[from + lane];
+    __syncwarp();
+    if (lane < n) sg.site[lane] = v;
+    __syncwarp();
 }
 
-template <bool EXACT, bool BANK>
-__global__ void __launch_bounds__(POOL_THREADS, 2) ev_pool(EvArgs a, uint32_t P) {
-    extern __shared__ __align__(16) unsigned char smem[];
+/* warp-aggregated append of the lanes in `m` to a queue: the lane's slot */
+__device__ __forceinline__ uint64_t queue_slot(unsigned long long* count, unsigned m, uint32_t lane) {
+    unsigned long long base = 0;
+    if (lane == 0 && m) base = atomicAdd(count, (unsigned long long)__popc(m));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    return base + __popc(m & ((1u << lane) - 1u));
+}
+
+__device__ __forceinline__ void flush_counters(const EvArgs& a, const Acc& acc, uint32_t lane) {
+    const unsigned long long kq = nrdev::warp_sum_u64(acc.kq);
+    const unsigned long long coll = nrdev::warp_sum_u64(acc.coll), virt = nrdev::warp_sum_u64(acc.virt);
+    const unsigned long long ab = nrdev::warp_sum_u64(acc.absorbed), lk = nrdev::warp_sum_u64(acc.leaked);
+    const unsigned long long cp = nrdev::warp_sum_u64(acc.capped);
+    if (lane == 0) {
+        GenState* s = a.stats;
+        if (kq) atomicAdd(&a.inst[0].st->kq, kq);
+        if (coll) atomicAdd(&s->collisions, coll);
+        if (virt) atomicAdd(&s->virtual_collisions, virt);
+        if (ab) atomicAdd(&s->absorbed, ab);
+        if (lk) atomicAdd(&s->leaked, lk);
+        if (cp) atomicAdd(&s->capped, cp);
+    }
+}
+
+template <bool FIRST, bool EXACT, bool BANK>
+__global__ void __launch_bounds__(256) ev_sort_flight(EvArgs a, int round) {
     nrdev::pdl_trigger();
     nrdev::pdl_wait();
-    __shared__ Hot s_h1;
-    __shared__ SrcBank s_src;
-    __shared__ uint32_t s_n[8];             /* live, next live, real, free, births, exhausted */
-    __shared__ unsigned long long s_base;
-    unsigned long long* prng = reinterpret_cast<unsigned long long*>(smem);
-    float* px = reinterpret_cast<float*>(prng + P);
-    float* pmu = px + P;
-    uint32_t* pev = reinterpret_cast<uint32_t*>(pmu + P);
-    uint32_t* pgs = pev + P;                /* group | site sequence << 8 */
-    uint32_t* pid = pgs + P;
-    uint32_t* preg = pid + P;               /* region of the pending real collision */
-    uint16_t* La = reinterpret_cast<uint16_t*>(preg + P);
-    uint16_t* Lb = La + P;
-    uint16_t* Rl = Lb + P;
-    uint16_t* Fl = Rl + P;
-    const size_t lists_end = (((size_t)(reinterpret_cast<unsigned char*>(Fl + P) - smem)) + 15) & ~(size_t)15;
-    PoolSite* s_site = reinterpret_cast<PoolSite*>(smem + lists_end);
-    unsigned char* tab = smem + lists_end + POOL_WARPS * sizeof(PoolSite);
     const EvInst& I = a.inst[0];
-    if (threadIdx.x == 0) {
-        load_hot(s_h1, I, 0, BANK);
-        if (BANK) {
-            const GenState* st = I.st;
-            s_src.bank = I.bank[st->gen & 1];
-            s_src.nbk = st->n_bank;
-            s_src.ndiv = I.ndiv;
-        }
-        s_n[0] = 0; s_n[1] = 0; s_n[2] = 0; s_n[3] = P; s_n[4] = 0; s_n[5] = 0;
-    }
-    for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) Fl[i] = (uint16_t)i;
-    TView tv;
-    stage_tables(I, tab, tv);
-    __syncthreads();
-    const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const unsigned lt = (1u << lane) - 1u;
+    const TView t = global_view(I);
+    const GenState* st = I.st;
+    const uint32_t lane = threadIdx.x & 31, G = t.G;
     const unsigned FULL = 0xffffffffu;
-    const uint32_t G = tv.G;
-    PoolSite& sg = s_site[w];
-    const uint32_t slab = (blockIdx.x * POOL_WARPS + w) % NSLAB;
-    uint32_t staged_sites = 0;
-    bool slab_full = false;
+    const uint64_t n_in = FIRST ? a.n_total : a.qcount[round - 1];
+    const int qin = (round - 1) & 1, qout = round & 1;
+    unsigned long long gseed = 0, nbk = 0;
+    const nraps_site* bank = nullptr;
+    if (FIRST) {
+        gseed = nr_generation_seed(I.seed, st->gen);
+        if (BANK) { nbk = st->n_bank; bank = I.bank[st->gen & 1]; }
+    }
     Acc acc = {0, 0, 0, 0, 0, 0};
-    const float inv_k = s_h1.inv_k;
-    const unsigned long long gseed = s_h1.gseed, hist_begin = s_h1.hist_begin;
-    double* const tally = s_h1.tally;
-    const uint32_t nc = s_h1.nc;
-    const uint64_t n_in = a.n_total;
-    uint16_t* L = La;
-    uint16_t* Ln = Lb;
-    /* warp-aggregated append of slot s to list `lst` with counter `cnt` */
-    auto append = [&](bool want, uint16_t s, uint16_t* lst, uint32_t* cnt) {
-        const unsigned m = __ballot_sync(FULL, want);
-        if (!m) return;
-        uint32_t base = 0;
-        if (lane == 0) base = atomicAdd(cnt, (uint32_t)__popc(m));
-        base = __shfl_sync(FULL, base, 0);
-        if (want) lst[base + __popc(m & lt)] = s;
-    };
-    /* a history ends: its site count for the bank order, counters */
-    auto end_history = [&](uint32_t id, uint32_t seq, int fate) {
-        if (fate == NRAPS_FATE_ABSORBED) acc.absorbed++;
-        else if (fate == NRAPS_FATE_LEAKED) acc.leaked++;
-        else { acc.capped++; atomicOr(&I.st->error, NR_ERR_CAPPED); }
-        if (BANK) a.count[id] = seq;
-    };
-    for (;;) {
-        /* ---- refill: births into free slots --------------------------------- */
-        if (threadIdx.x == 0) {
-            const uint32_t nf = s_n[3];
-            uint32_t got = 0;
-            unsigned long long base = 0;
-            if (!s_n[5] && nf) {
-                base = atomicAdd(&a.claim[0], (unsigned long long)nf);
-                if (base >= n_in) s_n[5] = 1;
-                else got = (uint32_t)((n_in - base) < nf ? (n_in - base) : nf);
-            }
-            s_base = base;
-            s_n[4] = got;
-        }
-        __syncthreads();
-        {
-            const uint32_t got = s_n[4], nl0 = s_n[0], nf = s_n[3];
-            const unsigned long long base = s_base;
-            for (uint32_t j = threadIdx.x; j < got; j += blockDim.x) {
-                const uint16_t slot = Fl[nf - got + j];
-                const uint64_t idx = base + j;
-                const uint32_t local = (uint32_t)(idx - hist_begin);
-                nr_pcg32 rng = nr_pcg32_seeded(gseed, local);
-                float bx = 0.0f, bmu;
-                uint32_t bg = 0;
-                bool banked = false;
-                if (BANK && s_src.nbk > 0) {
-                    const uint4 sv = reinterpret_cast<const uint4*>(s_src.bank)[bank_site(local, s_src.nbk, s_src.ndiv)];
-                    bx = __uint_as_float(sv.x); bg = sv.z; banked = true;
-                }
-                if (banked) {
-                    bmu = __fsub_rn(__fmul_rn(2.0f, u24(nr_pcg32_next(&rng))), 1.0f);
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i0 = (uint64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); i0 < n_in; i0 += stride) {
+        const uint64_t i = i0 + lane;
+        const bool valid = i < n_in;
+        float x = 0.0f, mu = 0.0f;
+        uint32_t id = 0, g = 0, seq = 0;
+        nr_pcg32 rng;
+        rng.state = 0; rng.inc = 1;
+        if (valid) {
+            if (FIRST) {
+                /* the birth of history i, as the warp transport's prefetch makes it */
+                id = (uint32_t)i;
+                rng = nr_pcg32_seeded(gseed, i);
+                if (BANK && nbk > 0) {
+                    const uint4 sv = reinterpret_cast<const uint4*>(bank)[bank_site(i, nbk, I.ndiv)];
+                    x = __uint_as_float(sv.x);
+                    mu = __fsub_rn(__fmul_rn(2.0f, u24(nr_pcg32_next(&rng))), 1.0f);
+                    const uint32_t c = sv.y < I.nc ? sv.y : I.nc - 1;
+                    g = count_below(I.chicdf + (uint32_t)I.cmat[c] * G, G, u24(nr_pcg32_next(&rng)));
                 } else {
                     const uint32_t cell = I.fuel[((uint64_t)nr_pcg32_next(&rng) * I.nfuel) >> 32];
                     const float sub = u24(nr_pcg32_next(&rng));
-                    bx = __fadd_rn(I.cleft[cell], __fmul_rn(sub, I.cdx[cell]));
-                    bmu = __fsub_rn(__fmul_rn(2.0f, u24(nr_pcg32_next(&rng))), 1.0f);
-                    bg = count_below(I.chicdf + (uint32_t)I.cmat[cell] * I.G, I.G, u24(nr_pcg32_next(&rng)));
+                    x = __fadd_rn(I.cleft[cell], __fmul_rn(sub, I.cdx[cell]));
+                    mu = __fsub_rn(__fmul_rn(2.0f, u24(nr_pcg32_next(&rng))), 1.0f);
+                    g = count_below(I.chicdf + (uint32_t)I.cmat[cell] * G, G, u24(nr_pcg32_next(&rng)));
                 }
-                px[slot] = bx; pmu[slot] = bmu; prng[slot] = rng.state; pev[slot] = 0;
-                pgs[slot] = bg; pid[slot] = (uint32_t)idx;
-                L[nl0 + j] = slot;
+            } else {
+                x = a.qx[qin][i]; mu = a.qmu[qin][i]; rng.state = a.qrng[qin][i]; id = a.qid[qin][i];
+                const uint32_t pk = a.qpk[qin][i];
+                g = pk & 15u; seq = pk >> 16;
+                rng.inc = ((uint64_t)id << 1) | 1ULL;
             }
         }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            s_n[0] += s_n[4];
-            s_n[3] -= s_n[4];
-            s_n[1] = 0;
-            s_n[2] = 0;
-        }
-        __syncthreads();
-        const uint32_t nL = s_n[0];
-        if (nL == 0 && s_n[5]) break;
-        /* ---- A: one flight per live particle -------------------------------- */
-        for (uint32_t b0 = w * 32; b0 < nL; b0 += blockDim.x) {
-            const uint32_t i = b0 + lane;
-            const bool valid = i < nL;
-            const uint16_t s = valid ? L[i] : 0;
-            int out = -1;                   /* 0 live, 1 real, 2 ended */
-            if (valid) {
-                float x = px[s], mu = pmu[s];
-                nr_pcg32 rng;
-                rng.state = prng[s];
-                const uint32_t id = pid[s];
-                rng.inc = ((uint64_t)(uint32_t)(id - hist_begin) << 1) | 1ULL;
-                const uint32_t gs = pgs[s], g = gs & 0xFFu;
-                const uint32_t ev = pev[s] + 1;
-                int fate = -1;
-                if (ev > a.max_events) {
-                    fate = NRAPS_FATE_CAPPED;
+        int fate = -1;
+        bool real = false;
+        uint32_t r = 0;
+        if (valid) {
+            const float d = __fmul_rn(neg_log<EXACT>(u24pos(nr_pcg32_next(&rng))), t.maj[G + g]);
+            x = __fadd_rn(x, __fmul_rn(mu, d));
+            int bounce = 0;
+            while (!(x >= 0.0f && x <= t.L)) {
+                if (x > t.L) {
+                    if (t.boundr > 0.0f) { x = __fsub_rn(t.L, __fsub_rn(x, t.L)); mu = -mu; }
+                    else { fate = NRAPS_FATE_LEAKED; break; }
                 } else {
-                    const float d = __fmul_rn(neg_log<EXACT>(u24pos(nr_pcg32_next(&rng))), tv.maj[G + g]);
-                    x = __fadd_rn(x, __fmul_rn(mu, d));
-                    int bounce = 0;
-                    while (!(x >= 0.0f && x <= tv.L)) {
-                        if (x > tv.L) {
-                            if (tv.boundr > 0.0f) { x = __fsub_rn(tv.L, __fsub_rn(x, tv.L)); mu = -mu; }
-                            else { fate = NRAPS_FATE_LEAKED; break; }
-                        } else {
-                            if (tv.boundl > 0.0f) { x = -x; mu = -mu; }
-                            else { fate = NRAPS_FATE_LEAKED; break; }
-                        }
-                        if (++bounce > 1000) { fate = NRAPS_FATE_CAPPED; break; }
-                    }
-                    if (fate < 0) {
-                        const uint32_t r = region_of(tv, x);
-                        const uint32_t m = tv.rmat[r];
-                        if (__fmul_rn(u24(nr_pcg32_next(&rng)), tv.maj[g]) < tv.xs[(m * G + g) * 4]) {
-                            out = 1;
-                            preg[s] = r;
-                        } else {
-                            out = 0;
-                            acc.virt++;
-                        }
-                    }
+                    if (t.boundl > 0.0f) { x = -x; mu = -mu; }
+                    else { fate = NRAPS_FATE_LEAKED; break; }
                 }
-                if (fate >= 0) {
-                    out = 2;
-                    end_history(id, gs >> 8, fate);
-                } else {
-                    px[s] = x; pmu[s] = mu; prng[s] = rng.state; pev[s] = ev;
-                }
+                if (++bounce > 1000) { fate = NRAPS_FATE_CAPPED; break; }
             }
-            append(out == 0, s, Ln, &s_n[1]);
-            append(out == 1, s, Rl, &s_n[2]);
-            append(out == 2, s, Fl, &s_n[3]);
+            if (fate < 0) {
+                r = region_of(t, x);
+                const uint32_t m = t.rmat[r];
+                real = __fmul_rn(u24(nr_pcg32_next(&rng)), t.maj[g]) < t.xs[m * G + g].x;
+                if (real) acc.coll++; else acc.virt++;
+            } else {
+                if (fate == NRAPS_FATE_LEAKED) acc.leaked++;
+                else { acc.capped++; atomicOr(&I.st->error, NR_ERR_CAPPED); }
+                if (BANK) a.count[id] = seq;
+            }
         }
-        __syncthreads();
-        /* ---- B: one real collision per particle of R ------------------------ */
-        const uint32_t nR = s_n[2];
-        for (uint32_t b0 = w * 32; b0 < nR; b0 += blockDim.x) {
-            const uint32_t i = b0 + lane;
-            const bool valid = i < nR;
-            const uint16_t s = valid ? Rl[i] : 0;
-            uint32_t pending = 0, cell = 0, m = 0, g = 0, seq = 0, id = 0;
-            float x = 0.0f;
-            nr_pcg32 rng;
-            rng.state = 0; rng.inc = 1;
-            if (valid) {
-                x = px[s];
-                rng.state = prng[s];
-                id = pid[s];
-                rng.inc = ((uint64_t)(uint32_t)(id - hist_begin) << 1) | 1ULL;
-                const uint32_t gs = pgs[s];
-                g = gs & 0xFFu;
-                seq = gs >> 8;
-                const uint32_t r = preg[s];
-                m = tv.rmat[r];
-                acc.coll++;
-                const float rel = __fmul_rn(__fsub_rn(x, tv.left[r]), tv.invdx[r]);
-                const uint32_t nr = tv.ncell[r];
-                uint32_t k = rel > 0.0f ? (uint32_t)rel : 0u;
-                if (k >= nr) k = nr - 1;
-                cell = tv.first[r] + k;
-                const uint32_t j = m * G + g;
-                nrdev::red_add_f64(&tally[(uint64_t)g * nc + cell], tv.inv_st64[j]);
-                acc.kq += tv.kq[j];
-                if (BANK) {
-                    const float nu = __fadd_rn(__fmul_rn(tv.xs[j * 4 + 2], inv_k), u24(nr_pcg32_next(&rng)));
-                    const int n = (int)floorf(nu);
-                    pending = n > 64 ? 64u : (uint32_t)n;
-                }
+        const unsigned vm = __ballot_sync(FULL, valid && fate < 0 && !real);
+        const unsigned rm = __ballot_sync(FULL, valid && real);
+        const uint64_t vo = queue_slot(&a.qcount[round], vm, lane);
+        const uint64_t ro = queue_slot(&a.ccount[round], rm, lane);
+        const uint32_t pk = g | (seq << 16);
+        if (valid && fate < 0) {
+            if (real) {
+                a.cx[ro] = x; a.cmu[ro] = mu; a.crng[ro] = rng.state; a.cid[ro] = id; a.cpk[ro] = pk;
+                a.creg[ro] = r;
+            } else {
+                a.qx[qout][vo] = x; a.qmu[qout][vo] = mu; a.qrng[qout][vo] = rng.state;
+                a.qid[qout][vo] = id; a.qpk[qout][vo] = pk;
             }
+        }
+    }
+    flush_counters(a, acc, lane);
+}
+
+template <bool BANK>
+__global__ void __launch_bounds__(256) ev_sort_collide(EvArgs a, int round) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    nrdev::pdl_trigger();
+    nrdev::pdl_wait();
+    const EvInst& I = a.inst[0];
+    const TView t = global_view(I);
+    const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5, G = t.G;
+    const unsigned lt = (1u << lane) - 1u;
+    const unsigned FULL = 0xffffffffu;
+    SiteStage& sg = reinterpret_cast<SiteStage*>(smem)[w];
+    const uint32_t slab = (blockIdx.x * (blockDim.x >> 5) + w) % NSLAB;
+    const uint64_t n_in = a.ccount[round];
+    const int qout = round & 1;
+    const float inv_k = BANK ? I.st->inv_kf : 0.0f;
+    double* tally = I.tally;
+    const uint32_t nc = I.nc;
+    uint32_t staged_sites = 0;
+    bool slab_full = false;
+    Acc acc = {0, 0, 0, 0, 0, 0};
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i0 = (uint64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); i0 < n_in; i0 += stride) {
+        const uint64_t i = i0 + lane;
+        const bool valid = i < n_in;
+        float x = 0.0f, mu = 0.0f;
+        uint32_t id = 0, g = 0, seq = 0, r = 0;
+        nr_pcg32 rng;
+        rng.state = 0; rng.inc = 1;
+        if (valid) {
+            x = a.cx[i]; mu = a.cmu[i]; rng.state = a.crng[i]; id = a.cid[i];
+            const uint32_t pk = a.cpk[i];
+            g = pk & 15u; seq = pk >> 16; r = a.creg[i];
+            rng.inc = ((uint64_t)id << 1) | 1ULL;
+        }
+        uint32_t pending = 0, cell = 0, j = 0;
+        if (valid) {
+            const uint32_t m = t.rmat[r];
+            j = m * G + g;
+            const float4 X = t.xs[j];
+            const float4 rd = t.rdat[r];
+            const float rel = __fmul_rn(__fsub_rn(x, rd.x), rd.y);
+            const uint32_t nr = __float_as_uint(rd.w);
+            uint32_t k = rel > 0.0f ? (uint32_t)rel : 0u;
+            if (k >= nr) k = nr - 1;
+            cell = __float_as_uint(rd.z) + k;
+            nrdev::red_add_f64(&tally[(uint64_t)g * nc + cell], t.inv_st64[j]);
+            acc.kq += t.kq[j];
             if (BANK) {
-                while (__any_sync(FULL, pending > 0)) {
-                    const unsigned sm = __ballot_sync(FULL, pending > 0);
-                    if (pending > 0) {
-                        const uint32_t sgp = count_below(tv.chi + m * G, G, u24(nr_pcg32_next(&rng)));
-                        const uint32_t slot = staged_sites + __popc(sm & lt);
-                        sg.site[slot] = make_uint4(__float_as_uint(x), cell | (sgp << 27), id, seq & 0xFFFFu);
-                        if (seq >= 0xFFFFu) atomicOr(&I.st->error, NR_ERR_CAPACITY);
-                        seq++;
-                        pending--;
-                    }
-                    staged_sites += __popc(sm);
-                    __syncwarp();
-                    if (staged_sites >= 32) {
-                        if (!flush_sites(a, sg, 32, slab, lane)) slab_full = true;
-                        uint4 v = make_uint4(0, 0, 0, 0);
-                        if (lane < staged_sites - 32) v = sg.site[32 + lane];
-                        __syncwarp();
-                        if (lane < staged_sites - 32) sg.site[lane] = v;
-                        __syncwarp();
-                        staged_sites -= 32;
-                    }
-                }
+                const float nu = __fadd_rn(__fmul_rn(X.z, inv_k), u24(nr_pcg32_next(&rng)));
+                const int n = (int)floorf(nu);
+                pending = n > 64 ? 64u : (uint32_t)n;
             }
-            int out = -1;                   /* 0 live, 2 ended */
-            if (valid) {
-                const uint32_t j = m * G + g;
-                if (u24(nr_pcg32_next(&rng)) < tv.xs[j * 4 + 1]) {
-                    out = 2;
-                    end_history(id, seq, NRAPS_FATE_ABSORBED);
-                } else {
-                    const uint32_t ng = count_le(tv.scdf + j * G, G, u24(nr_pcg32_next(&rng)));
-                    pmu[s] = __fsub_rn(__fmul_rn(2.0f, u24(nr_pcg32_next(&rng))), 1.0f);
-                    pgs[s] = ng | (seq << 8);
-                    prng[s] = rng.state;
-                    out = 0;
-                }
-            }
-            append(out == 0, s, Ln, &s_n[1]);
-            append(out == 2, s, Fl, &s_n[3]);
         }
-        __syncthreads();
-        /* ---- the next live list --------------------------------------------- */
-        uint16_t* t2 = L; L = Ln; Ln = t2;
-        if (threadIdx.x == 0) s_n[0] = s_n[1];
-        __syncthreads();
+        if (BANK) {
+            while (__any_sync(FULL, pending > 0)) {
+                const unsigned sm = __ballot_sync(FULL, pending > 0);
+                if (pending > 0) {
+                    const uint32_t slot = staged_sites + __popc(sm & lt);
+                    sg.site[slot] = make_uint4(__float_as_uint(x), cell, id, seq & 0xFFFFu);
+                    if (seq >= 0xFFFFu) atomicOr(&I.st->error, NR_ERR_CAPACITY);
+                    seq++;
+                    pending--;
+                }
+                staged_sites += __popc(sm);
+                __syncwarp();
+                if (staged_sites >= 32) {
+                    if (!flush_sites(a, sg, 32, slab, lane)) slab_full = true;
+                    move_sites_down(sg, 32, staged_sites - 32, lane);
+                    staged_sites -= 32;
+                }
+            }
+        }
+        bool scattered = false;
+        if (valid) {
+            const uint32_t o = count_outcome(t.ocdf + j * G, G, u24(nr_pcg32_next(&rng)));
+            if (o == 0) {
+                acc.absorbed++;
+                if (BANK) a.count[id] = seq;
+            } else {
+                g = o - 1;
+                mu = __fsub_rn(__fmul_rn(2.0f, u24(nr_pcg32_next(&rng))), 1.0f);
+                scattered = true;
+            }
+        }
+        const unsigned smk = __ballot_sync(FULL, scattered);
+        const uint64_t so = queue_slot(&a.qcount[round], smk, lane);
+        if (scattered) {
+            a.qx[qout][so] = x; a.qmu[qout][so] = mu; a.qrng[qout][so] = rng.state;
+            a.qid[qout][so] = id; a.qpk[qout][so] = g | (seq << 16);
+        }
     }
-    if (BANK && staged_sites) { if (!flush_sites(a, sg, staged_sites, slab, lane)) slab_full = true; }
+    __syncwarp();
+    if (BANK && staged_sites && !flush_sites(a, sg, staged_sites, slab, lane)) slab_full = true;
     if (slab_full && lane == 0) atomicOr(&I.st->error, NR_ERR_CAPACITY);
-    unsigned long long kq = nrdev::warp_sum_u64(acc.kq);
-    unsigned long long coll = nrdev::warp_sum_u64(acc.coll), virt = nrdev::warp_sum_u64(acc.virt);
-    unsigned long long ab = nrdev::warp_sum_u64(acc.absorbed), lk = nrdev::warp_sum_u64(acc.leaked);
-    unsigned long long cp = nrdev::warp_sum_u64(acc.capped);
-    if (lane == 0) {
-        GenState* st = a.stats;
-        if (kq) atomicAdd(&I.st->kq, kq);
-        if (coll) atomicAdd(&st->collisions, coll);
-        if (virt) atomicAdd(&st->virtual_collisions, virt);
-        if (ab) atomicAdd(&st->absorbed, ab);
-        if (lk) atomicAdd(&st->leaked, lk);
-        if (cp) atomicAdd(&st->capped, cp);
-    }
+    flush_counters(a, acc, lane);
 }
 
 __device__ __forceinline__ uint32_t find_inst(const uint64_t* begin, uint32_t n, uint64_t i) {
@@ -1537,6 +1503,7 @@ __global__ void __launch_bounds__(RB_THREADS) ev_rb_scatter(EvArgs a) {
    generation (called by the block that closes a generation) */
 __device__ __forceinline__ void reset_pass_counters(const EvArgs& a) {
     for (uint32_t p = threadIdx.x; p < 2 * (MAX_PASSES + 2); p += blockDim.x) a.qcount[p] = 0;
+    for (uint32_t p = threadIdx.x; p < MAX_PASSES + 2; p += blockDim.x) a.ccount[p] = 0;
     if (threadIdx.x == 0) *a.rb_next = 0;
     for (uint32_t q = threadIdx.x; q < NSLAB; q += blockDim.x) a.slab_count[q] = 0;
 }
@@ -1753,14 +1720,27 @@ __global__ void __launch_bounds__(FIN_THREADS) ev_finalize(EvArgs a) {
 template <class T> struct DBuf {
     T* p = nullptr;
     size_t n = 0;
+    cudaStream_t fs = nullptr;       /* pooled: freed in this stream's order */
+    bool pooled = false;
     DBuf() = default;
     DBuf(const DBuf&) = delete;
     DBuf& operator=(const DBuf&) = delete;
-    ~DBuf() { if (p) cudaFree(p); }
-    cudaError_t alloc(size_t count) {
-        if (p) { cudaFree(p); p = nullptr; }
+    ~DBuf() { release(); }
+    void release() {
+        if (p) { if (pooled) cudaFreeAsync(p, fs); else cudaFree(p); }
+        p = nullptr;
+        pooled = false;
+    }
+    cudaError_t alloc(size_t count, cudaMemPool_t pool = nullptr, cudaStream_t s = nullptr) {
+        release();
         n = count;
-        return count ? cudaMalloc(&p, count * sizeof(T)) : cudaSuccess;
+        if (!count) return cudaSuccess;
+        if (pool) {
+            pooled = true;
+            fs = s;
+            return cudaMallocFromPoolAsync(reinterpret_cast<void**>(&p), count * sizeof(T), pool, s);
+        }
+        return cudaMalloc(&p, count * sizeof(T));
     }
 };
 
@@ -1792,7 +1772,11 @@ struct EventEngine::Impl {
     EvArgs args{};
     bool committed = false;
     int grid_blocks = 0;
-    int pool_grid = 0;          /* resident blocks of the pool transport        */
+    /* sorted transport: the collision queue and the grid of its kernels */
+    DBuf<float> cx, cmu;
+    DBuf<unsigned long long> crng;
+    DBuf<uint32_t> cid, cpk, creg;
+    int sort_grid = 0;          /* resident blocks of the sorted kernels (0: not in use) */
     /* ranged launches stage the tables in shared memory when every
        instance's fit, else read them from global memory */
     bool ranged_fit = false;
@@ -1813,6 +1797,9 @@ struct EventEngine::Impl {
        kernel's launch and prologue overlap the previous kernel's tail);
        NRAPS_NO_PDL=1 in the environment turns it off */
     bool pdl = !(std::getenv("NRAPS_NO_PDL") && std::getenv("NRAPS_NO_PDL")[0] == '1');
+    /* per-instance tables from a stream-ordered pool (set_pool), or cudaMalloc */
+    cudaMemPool_t pool = nullptr;
+    cudaStream_t pool_stream = nullptr;
     ~Impl() { for (Inst* i : inst) delete i; }
 };
 
@@ -1828,16 +1815,19 @@ int EventEngine::configure(const nraps_opts& o, std::string& err) {
     if (o.events_per_pass) params.K = o.events_per_pass;
     if (o.passes) params.passes = o.passes;
     params.tail = o.tail_lanes;
-    params.pool = o.pool_slots;
+    params.sort = o.sort_rounds;
     params.range = o.range_len;
     if (params.range && (params.range < 64 || params.range > RB_MAX_RANGE)) { err = "range_len must be in [64, 32768]"; return NRAPS_ERR_INVALID; }
-    if (params.range) { params.K = NRAPS_ONE_PASS; params.passes = 0; params.tail = 0; params.pool = 0; }
-    if (params.pool && (params.pool < 64 || params.pool > POOL_MAX)) { err = "pool_slots must be in [64, 4096]"; return NRAPS_ERR_INVALID; }
-    if (params.pool) { params.K = NRAPS_ONE_PASS; params.passes = 0; params.tail = 0; params.block = POOL_THREADS; }
+    if (params.range) { params.K = NRAPS_ONE_PASS; params.passes = 0; params.tail = 0; params.sort = 0; }
+    if (params.sort > MAX_PASSES) { err = "sort_rounds must be at most 16"; return NRAPS_ERR_INVALID; }
+    if (params.sort) { params.K = NRAPS_ONE_PASS; params.passes = 0; params.tail = 0; }
     if (params.K == NRAPS_ONE_PASS && o.passes == 0) params.passes = 0;  /* every particle to its end in one pass */
     if (params.tail > 32) { err = "tail_lanes must be at most 32"; return NRAPS_ERR_INVALID; }
     if (params.tail && params.passes == 0) { err = "tail_lanes needs a following pass (passes >= 1)"; return NRAPS_ERR_INVALID; }
-    if (params.block != 128 && params.block != 256) { err = "block_size must be 128 or 256 for WOODCOCK"; return NRAPS_ERR_INVALID; }
+    if (params.block != 128 && params.block != 256 && !(params.block == 512 && params.range)) {
+        err = "block_size must be 128 or 256 for WOODCOCK (512 with range_len)";
+        return NRAPS_ERR_INVALID;
+    }
     if ((params.passes < 1 && params.K != NRAPS_ONE_PASS) || params.passes > MAX_PASSES) { err = "passes must be in [1, 16]"; return NRAPS_ERR_INVALID; }
     if (params.K < 1) { err = "events_per_pass must be >= 1"; return NRAPS_ERR_INVALID; }
     impl_->committed = false;
@@ -1846,8 +1836,12 @@ int EventEngine::configure(const nraps_opts& o, std::string& err) {
 
 uint64_t EventEngine::table_bytes(const nraps_problem& p) {
     uint64_t M = p.variables.mattypes, G = p.variables.energygroups, nc = p.mesh.n_cells;
-    return (M * G * (4 + G + 1) + 2 * G) * 4 + M * G * 16 + M * G * 8 + p.n_fuel * 4 +
-           nc * (4 + 4 + 1 + 8) + nc * (4 + 4 + 4 + 4 + 1) + 16384 * 2 + 20 * 256;
+    /* xs, outcome and chi CDFs, majorants, flux and k scores, fuel list, per
+       cell (left, width, material, nu*sigf-free FP64 width and inverse), per
+       region at most one per cell (16 B + material), bins (8 B each, at most
+       16384), 256-byte alignment of 17 arrays */
+    return (M * G * (4 + G + 1) + 2 * G) * 4 + M * G * 16 + p.n_fuel * 4 +
+           nc * (4 + 4 + 1 + 8 + 8) + (nc + 1) * (16 + 1) + 16384 * 8 + 17 * 256;
 }
 
 int EventEngine::add_instance(const nraps_problem& p, const EvBuffers& b, std::string& err) {
@@ -1858,35 +1852,41 @@ int EventEngine::add_instance(const nraps_problem& p, const EvBuffers& b, std::s
     size_t off = 0;
     auto take = [&](size_t bytes) { size_t o = off; off = (off + bytes + 255) & ~(size_t)255; return o; };
     size_t o_xs = take(h.xs.size() * 4), o_inv64 = take(h.inv_st64.size() * 8), o_kq = take(h.kq.size() * 8);
-    size_t o_scdf = take(h.scdf.size() * 4), o_chi = take(h.chicdf.size() * 4);
-    size_t o_maj = take(h.maj.size() * 4), o_left = take(h.rleft.size() * 4), o_invdx = take(h.rinvdx.size() * 4);
-    size_t o_rmat = take(h.rmat.size()), o_rfirst = take(h.rfirst.size() * 4), o_rn = take(h.rncell.size() * 4);
-    size_t o_grid = take(h.grid.size() * 2), o_fuel = take(h.fuel.size() * 4), o_cleft = take(h.cleft.size() * 4);
+    size_t o_ocdf = take(h.ocdf.size() * 4), o_chi = take(h.chicdf.size() * 4);
+    size_t o_maj = take(h.maj.size() * 4), o_rdat = take(h.rdat.size() * 4);
+    size_t o_rmat = take(h.rmat.size()), o_bins = take(h.bins.size() * 4);
+    size_t o_fuel = take(h.fuel.size() * 4), o_cleft = take(h.cleft.size() * 4);
     size_t o_cdx = take(h.cdx.size() * 4), o_cmat = take(h.cmat.size()), o_nsf = take(h.nsf64.size() * 8);
     size_t o_idx = take(h.inv_dx64.size() * 8);
     std::vector<unsigned char> host(off, 0);
     auto put = [&](size_t o, const void* src, size_t bytes) { if (bytes) std::memcpy(host.data() + o, src, bytes); };
     put(o_xs, h.xs.data(), h.xs.size() * 4); put(o_inv64, h.inv_st64.data(), h.inv_st64.size() * 8);
     put(o_kq, h.kq.data(), h.kq.size() * 8);
-    put(o_scdf, h.scdf.data(), h.scdf.size() * 4);
+    put(o_ocdf, h.ocdf.data(), h.ocdf.size() * 4);
     put(o_chi, h.chicdf.data(), h.chicdf.size() * 4); put(o_maj, h.maj.data(), h.maj.size() * 4);
-    put(o_left, h.rleft.data(), h.rleft.size() * 4); put(o_invdx, h.rinvdx.data(), h.rinvdx.size() * 4);
-    put(o_rmat, h.rmat.data(), h.rmat.size()); put(o_rfirst, h.rfirst.data(), h.rfirst.size() * 4);
-    put(o_rn, h.rncell.data(), h.rncell.size() * 4); put(o_grid, h.grid.data(), h.grid.size() * 2);
+    put(o_rdat, h.rdat.data(), h.rdat.size() * 4);
+    put(o_rmat, h.rmat.data(), h.rmat.size()); put(o_bins, h.bins.data(), h.bins.size() * 4);
     put(o_fuel, h.fuel.data(), h.fuel.size() * 4); put(o_cleft, h.cleft.data(), h.cleft.size() * 4);
     put(o_cdx, h.cdx.data(), h.cdx.size() * 4); put(o_cmat, h.cmat.data(), h.cmat.size());
     put(o_nsf, h.nsf64.data(), h.nsf64.size() * 8); put(o_idx, h.inv_dx64.data(), h.inv_dx64.size() * 8);
-    cudaError_t e = in->blob.alloc(off);
-    if (e == cudaSuccess) e = cudaMemcpy(in->blob.p, host.data(), off, cudaMemcpyHostToDevice);
+    cudaError_t e;
+    if (impl_->pool) {
+        /* stream-ordered: no device-wide synchronisation per instance; the
+           pageable source is staged before the copy call returns */
+        e = in->blob.alloc(off, impl_->pool, impl_->pool_stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(in->blob.p, host.data(), off, cudaMemcpyHostToDevice, impl_->pool_stream);
+    } else {
+        e = in->blob.alloc(off);
+        if (e == cudaSuccess) e = cudaMemcpy(in->blob.p, host.data(), off, cudaMemcpyHostToDevice);
+    }
     if (e != cudaSuccess) { err = std::string("event tables: ") + cudaGetErrorString(e); delete in; return -1; }
     unsigned char* B = in->blob.p;
     EvInst& d = in->d;
     d.xs = (const float*)(B + o_xs); d.inv_st64 = (const double*)(B + o_inv64);
     d.kq = (const unsigned long long*)(B + o_kq);
-    d.scdf = (const float*)(B + o_scdf); d.chicdf = (const float*)(B + o_chi);
-    d.maj = (const float*)(B + o_maj); d.rleft = (const float*)(B + o_left); d.rinvdx = (const float*)(B + o_invdx);
-    d.rmat = B + o_rmat; d.rfirst = (const uint32_t*)(B + o_rfirst); d.rncell = (const uint32_t*)(B + o_rn);
-    d.grid = (const uint16_t*)(B + o_grid); d.fuel = (const uint32_t*)(B + o_fuel);
+    d.ocdf = (const float*)(B + o_ocdf); d.chicdf = (const float*)(B + o_chi);
+    d.maj = (const float*)(B + o_maj); d.rdat = (const float4*)(B + o_rdat);
+    d.rmat = B + o_rmat; d.bins = (const uint2*)(B + o_bins); d.fuel = (const uint32_t*)(B + o_fuel);
     d.cleft = (const float*)(B + o_cleft); d.cdx = (const float*)(B + o_cdx); d.cmat = B + o_cmat;
     d.nsf64 = (const double*)(B + o_nsf); d.inv_dx64 = (const double*)(B + o_idx);
     d.M = h.M; d.G = h.G; d.R = h.R; d.nc = h.nc; d.nbins = h.nbins; d.nfuel = h.nfuel;
@@ -1918,6 +1918,7 @@ void EventEngine::clear_instances() {
 }
 
 uint32_t EventEngine::n_instances() const { return (uint32_t)impl_->inst.size(); }
+void EventEngine::set_pool(cudaMemPool_t pool, cudaStream_t s) { impl_->pool = pool; impl_->pool_stream = s; }
 void EventEngine::set_records(nraps_history_record* rec) { impl_->rec = rec; impl_->committed = false; }
 const uint32_t* EventEngine::offsets() const { return impl_->offsets.p; }
 uint64_t EventEngine::n_total() const { return impl_->n_total; }
@@ -1930,11 +1931,11 @@ uint64_t EventEngine::shared_bytes() const {
 }
 
 namespace {
-template <bool SOURCE, int ONE, bool EXACT, bool BANK, bool REC>
+template <bool SOURCE, int ONE, bool EXACT, bool BANK, bool REC, bool OP>
 void set_smem_attr(size_t smem) {
     static size_t granted = 48 * 1024;          /* the default dynamic limit         */
     if (smem > granted) {
-        cudaFuncSetAttribute(pass_kernel<SOURCE, ONE, EXACT, BANK, REC>(),
+        cudaFuncSetAttribute(pass_kernel<SOURCE, ONE, EXACT, BANK, REC, OP>(),
                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         granted = smem;
     }
@@ -1948,16 +1949,24 @@ int launch_passes(const EvArgs& a, const EvParams& prm, int grid, size_t smem, u
     smem += stage_bytes(block);
     unsigned g0 = (unsigned)std::min<uint64_t>((n_total + block - 1) / block, (uint64_t)grid);
     if (g0 == 0) g0 = 1;
-    set_smem_attr<true, ONE, EXACT, BANK, REC>(smem);
-    set_smem_attr<false, ONE, EXACT, BANK, REC>(smem);
     uint32_t P = prm.passes;
-    if (launch_k(pdl, pass_kernel<true, ONE, EXACT, BANK, REC>(), dim3(g0), dim3(block), smem, s, a, 0,
-                 P == 0 ? 0xFFFFFFFFu : prm.K, P == 0 ? 0u : prm.tail) != cudaSuccess)
-        return -1;
+    cudaError_t e;
+    if (P == 0) {
+        /* one pass: every particle runs to its end */
+        set_smem_attr<true, ONE, EXACT, BANK, REC, true>(smem);
+        e = launch_k(pdl, pass_kernel<true, ONE, EXACT, BANK, REC, true>(), dim3(g0), dim3(block), smem, s, a, 0,
+                     0xFFFFFFFFu, 0u);
+    } else {
+        set_smem_attr<true, ONE, EXACT, BANK, REC, false>(smem);
+        set_smem_attr<false, ONE, EXACT, BANK, REC, false>(smem);
+        e = launch_k(pdl, pass_kernel<true, ONE, EXACT, BANK, REC, false>(), dim3(g0), dim3(block), smem, s, a, 0,
+                     prm.K, prm.tail);
+    }
+    if (e != cudaSuccess) return -1;
     ++launched;
     for (uint32_t p = 1; p <= P; ++p) {
         const bool last = p == P;
-        if (launch_k(pdl, pass_kernel<false, ONE, EXACT, BANK, REC>(), dim3((unsigned)grid), dim3(block), smem, s, a,
+        if (launch_k(pdl, pass_kernel<false, ONE, EXACT, BANK, REC, false>(), dim3((unsigned)grid), dim3(block), smem, s, a,
                      (int)p, last ? 0xFFFFFFFFu : prm.K, last ? 0u : prm.tail) != cudaSuccess)
             return -1;
         ++launched;
@@ -2006,14 +2015,17 @@ int EventEngine::commit(cudaStream_t s, std::string& err) {
         A(m.count.alloc(c)); A(m.offsets.alloc(c + 1));
         A(m.block_sums.alloc((c + 4095) / 4096 + 1));
     }
-    if (!m.qcount.p) { A(m.qcount.alloc(2 * (MAX_PASSES + 2) + 2)); A(m.slab_count.alloc(NSLAB)); A(m.bstats.alloc(1)); }
+    /* pass fills and claims, the finalize block count, the ranged bank's
+       chunk count, the sorted rounds' collision-queue fills */
+    constexpr size_t NCOUNT = 3 * (MAX_PASSES + 2) + 2;
+    if (!m.qcount.p) { A(m.qcount.alloc(NCOUNT)); A(m.slab_count.alloc(NSLAB)); A(m.bstats.alloc(1)); }
     /* slabs: room for every banked site plus one partial flush per warp */
     uint64_t want_slab = bank ? (bank_sum + 2 * m.n_total) / NSLAB + 8192 : 64;
     if (want_slab > m.slab_cap || !m.sites.p) {
         m.slab_cap = std::max<uint64_t>(want_slab, m.slab_cap + m.slab_cap / 2);
         A(m.sites.alloc(NSLAB * m.slab_cap));
     }
-    A(cudaMemsetAsync(m.qcount.p, 0, (2 * (MAX_PASSES + 2) + 2) * 8, s));
+    A(cudaMemsetAsync(m.qcount.p, 0, NCOUNT * 8, s));
     A(cudaMemsetAsync(m.slab_count.p, 0, NSLAB * 8, s));
     A(cudaMemsetAsync(m.bstats.p, 0, sizeof(GenState), s));
     if (bank && m.n_total) A(cudaMemsetAsync(m.count.p, 0, m.n_total * 4, s));
@@ -2031,6 +2043,7 @@ int EventEngine::commit(cudaStream_t s, std::string& err) {
     a.slab_count = m.slab_count.p; a.slab_cap = m.slab_cap;
     a.rb = 0;
     a.rb_next = m.qcount.p + 2 * (MAX_PASSES + 2) + 1;
+    a.ccount = m.qcount.p + 2 * (MAX_PASSES + 2) + 2;
     a.rb_pool_chunks = 0;
     a.rb_chunk = nullptr; a.rb_fill = nullptr; a.rb_base = nullptr; a.rb_total = nullptr;
     a.count = m.count.p; a.offsets = m.offsets.p;
@@ -2118,32 +2131,40 @@ int EventEngine::size_grid() {
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     /* persistent grid: as many blocks as are resident at once */
     int per_sm = 0;
-    const void* fn = m.one ? (m.exact ? (const void*)pass_kernel<false, 1, true, true, false>()
-                                      : (const void*)pass_kernel<false, 1, false, true, false>())
-                           : (const void*)pass_kernel<false, 0, false, true, false>();
+    const void* fn = m.one ? (m.exact ? (const void*)pass_kernel<true, 1, true, true, false, true>()
+                                      : (const void*)pass_kernel<true, 1, false, true, false, true>())
+                           : (const void*)pass_kernel<true, 0, false, true, false, true>();
     const size_t dyn = stage_bytes(params.block) + (m.one ? m.smem_bytes : 0);
     if (dyn > 48 * 1024) cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, (int)params.block, dyn) != cudaSuccess ||
         per_sm < 1)
         per_sm = 1;
     m.grid_blocks = sms * per_sm;
-    m.pool_grid = 0;
-    if (m.one && params.pool && m.rec == nullptr) {
-        const void* pf = m.exact ? (m.mode == NRAPS_MODE_BANK ? (const void*)ev_pool<true, true> : (const void*)ev_pool<true, false>)
-                                 : (m.mode == NRAPS_MODE_BANK ? (const void*)ev_pool<false, true> : (const void*)ev_pool<false, false>);
-        const size_t pdyn = pool_bytes(params.pool) + m.smem_bytes;
-        int pb = 0;
-        if (pdyn <= 227 * 1024) {
-            cudaFuncSetAttribute(pf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pdyn);
-            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pb, pf, POOL_THREADS, pdyn) != cudaSuccess) pb = 0;
+    /* sorted transport (one instance, no records): the collision queue, and
+       a persistent grid for its kernels */
+    m.sort_grid = 0;
+    if (m.one && params.sort && m.rec == nullptr) {
+        if (m.cx.n < m.n_total) {
+            cudaError_t e = cudaSuccess;
+            auto A = [&](cudaError_t x) { if (e == cudaSuccess) e = x; };
+            A(m.cx.alloc(m.cap_total)); A(m.cmu.alloc(m.cap_total)); A(m.crng.alloc(m.cap_total));
+            A(m.cid.alloc(m.cap_total)); A(m.cpk.alloc(m.cap_total)); A(m.creg.alloc(m.cap_total));
+            if (e != cudaSuccess) return NRAPS_ERR_NOMEM;
         }
-        m.pool_grid = sms * pb;     /* 0: the pool does not fit, ev_pass runs */
+        EvArgs& a = m.args;
+        a.cx = m.cx.p; a.cmu = m.cmu.p; a.crng = m.crng.p; a.cid = m.cid.p; a.cpk = m.cpk.p; a.creg = m.creg.p;
+        int pb = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pb, ev_sort_collide<true>, 256, SORT_STAGE_BYTES) != cudaSuccess ||
+            pb < 1)
+            pb = 1;
+        m.sort_grid = sms * pb;
     }
     return NRAPS_OK;
 }
 
 uint64_t EventEngine::launches_per_generation() const {
-    return (impl_->pool_grid || params.passes == 0) ? 1 : 1 + params.passes;
+    if (impl_->sort_grid) return 2 * (uint64_t)params.sort + 1;
+    return params.passes == 0 ? 1 : 1 + params.passes;
 }
 
 int EventEngine::enqueue_generation(cudaStream_t s, bool with_finalize, cudaEvent_t t0, cudaEvent_t t1) {
@@ -2179,35 +2200,60 @@ int EventEngine::enqueue_generation(cudaStream_t s, bool with_finalize, cudaEven
         if (m.ranged_fit) {
             const size_t rs = stage_bytes(params.block) + m.ranged_smem;
 #define EV_RANGED(EXACT, BANK) \
-    set_smem_attr<true, 2, EXACT, BANK, false>(rs); \
-    launch_k(m.pdl, ev_pass<true, 2, EXACT, BANK, false>, dim3(m.ranged_blocks), dim3(params.block), rs, s, ar, 0, \
-             0xFFFFFFFFu, 0u)
+    if (params.block == 512) { \
+        cudaFuncSetAttribute(ev_pass_wide<2, EXACT, BANK>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rs); \
+        launch_k(m.pdl, ev_pass_wide<2, EXACT, BANK>, dim3(m.ranged_blocks), dim3(512), rs, s, ar, 0, 0xFFFFFFFFu, 0u); \
+    } else { \
+        set_smem_attr<true, 2, EXACT, BANK, false, true>(rs); \
+        launch_k(m.pdl, ev_pass<true, 2, EXACT, BANK, false, true>, dim3(m.ranged_blocks), dim3(params.block), rs, s, \
+                 ar, 0, 0xFFFFFFFFu, 0u); \
+    }
             if (bank) { if (m.exact) { EV_RANGED(true, true); } else { EV_RANGED(false, true); } }
             else { if (m.exact) { EV_RANGED(true, false); } else { EV_RANGED(false, false); } }
 #undef EV_RANGED
         } else {
             const size_t rs = stage_bytes(params.block);
 #define EV_RANGED(EXACT, BANK) \
-    set_smem_attr<true, 3, EXACT, BANK, false>(rs); \
-    launch_k(m.pdl, ev_pass<true, 3, EXACT, BANK, false>, dim3(m.ranged_blocks), dim3(params.block), rs, s, ar, 0, \
-             0xFFFFFFFFu, 0u)
+    if (params.block == 512) { \
+        cudaFuncSetAttribute(ev_pass_wide<3, EXACT, BANK>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rs); \
+        launch_k(m.pdl, ev_pass_wide<3, EXACT, BANK>, dim3(m.ranged_blocks), dim3(512), rs, s, ar, 0, 0xFFFFFFFFu, 0u); \
+    } else { \
+        set_smem_attr<true, 3, EXACT, BANK, false, true>(rs); \
+        launch_k(m.pdl, ev_pass<true, 3, EXACT, BANK, false, true>, dim3(m.ranged_blocks), dim3(params.block), rs, s, \
+                 ar, 0, 0xFFFFFFFFu, 0u); \
+    }
             if (bank) { if (m.exact) { EV_RANGED(true, true); } else { EV_RANGED(false, true); } }
             else { if (m.exact) { EV_RANGED(true, false); } else { EV_RANGED(false, false); } }
 #undef EV_RANGED
         }
         r = cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
-    } else if (m.one && m.pool_grid) {
-        const size_t pdyn = pool_bytes(params.pool) + m.smem_bytes;
-        const unsigned pg = (unsigned)std::min<uint64_t>((m.n_total + params.pool - 1) / params.pool,
-                                                         (uint64_t)m.pool_grid);
-        if (bank) {
-            if (m.exact) launch_k(m.pdl, ev_pool<true, true>, dim3(pg ? pg : 1), dim3(POOL_THREADS), pdyn, s, a, params.pool);
-            else launch_k(m.pdl, ev_pool<false, true>, dim3(pg ? pg : 1), dim3(POOL_THREADS), pdyn, s, a, params.pool);
-        } else {
-            if (m.exact) launch_k(m.pdl, ev_pool<true, false>, dim3(pg ? pg : 1), dim3(POOL_THREADS), pdyn, s, a, params.pool);
-            else launch_k(m.pdl, ev_pool<false, false>, dim3(pg ? pg : 1), dim3(POOL_THREADS), pdyn, s, a, params.pool);
+    } else if (m.one && m.sort_grid) {
+        const uint32_t R = params.sort;
+        const dim3 sg((unsigned)m.sort_grid), sb(256);
+        for (uint32_t rd = 0; rd < R; ++rd) {
+#define EV_SORT_FLIGHT(FIRST, EXACT, BANK) launch_k(m.pdl, ev_sort_flight<FIRST, EXACT, BANK>, sg, sb, 0, s, a, (int)rd)
+            if (rd == 0) {
+                if (bank) { if (m.exact) EV_SORT_FLIGHT(true, true, true); else EV_SORT_FLIGHT(true, false, true); }
+                else { if (m.exact) EV_SORT_FLIGHT(true, true, false); else EV_SORT_FLIGHT(true, false, false); }
+            } else {
+                if (bank) { if (m.exact) EV_SORT_FLIGHT(false, true, true); else EV_SORT_FLIGHT(false, false, true); }
+                else { if (m.exact) EV_SORT_FLIGHT(false, true, false); else EV_SORT_FLIGHT(false, false, false); }
+            }
+#undef EV_SORT_FLIGHT
+            if (bank) launch_k(m.pdl, ev_sort_collide<true>, sg, sb, SORT_STAGE_BYTES, s, a, (int)rd);
+            else launch_k(m.pdl, ev_sort_collide<false>, sg, sb, SORT_STAGE_BYTES, s, a, (int)rd);
         }
-        r = cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
+        /* the survivors of the last round run to their ends: pass R reads
+           round R-1's output queue */
+        const size_t smem = stage_bytes(params.block) + m.smem_bytes;
+#define EV_SORT_TAIL(EXACT, BANK) \
+    set_smem_attr<false, 1, EXACT, BANK, false, false>(smem); \
+    launch_k(m.pdl, pass_kernel<false, 1, EXACT, BANK, false, false>(), dim3((unsigned)m.grid_blocks), \
+             dim3(params.block), smem, s, a, (int)R, 0xFFFFFFFFu, 0u)
+        if (bank) { if (m.exact) { EV_SORT_TAIL(true, true); } else { EV_SORT_TAIL(false, true); } }
+        else { if (m.exact) { EV_SORT_TAIL(true, false); } else { EV_SORT_TAIL(false, false); } }
+#undef EV_SORT_TAIL
+        r = cudaPeekAtLastError() == cudaSuccess ? (int)(2 * R + 1) : -1;
     } else if (m.one) {
         if (bank) { if (m.exact) EV_LAUNCH(true, true, true, false); else EV_LAUNCH(true, false, true, false); }
         else { if (m.exact) EV_LAUNCH(true, true, false, false); else EV_LAUNCH(true, false, false, false); }

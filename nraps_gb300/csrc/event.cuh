@@ -5,7 +5,9 @@
  * fixed sequence of launches:
  *   pass 0      every source particle is born (from its instance's ordered
  *               fission bank, or the uniform fuel source) and runs up to K
- *               real collisions; survivors are compacted into queue 0;
+ *               real collisions; survivors are compacted into queue 0
+ *               (or, sorted: R rounds of one flight kernel and one
+ *               collision kernel over event-type queues);
  *   pass 1..P-1 the queued particles run K more real collisions each and
  *               the survivors are compacted into the other queue;
  *   drain       the last queue runs to completion;
@@ -52,8 +54,9 @@ struct EvParams {
     uint32_t K = 4;         /* real collisions per particle per queue pass     */
     uint32_t passes = 3;    /* queue passes before the drain pass; 0 = one
                                pass that runs every particle to its end      */
-    uint32_t pool = 0;      /* > 0: the pool transport with this many particle
-                               slots per block (one pass; single instance) */
+    uint32_t sort = 0;      /* > 0: the sorted transport (single instance): this
+                               many rounds of flight and collision kernels over
+                               event-type queues, then one pass for the rest */
     uint32_t range = 0;     /* > 0 (one pass): a ranged launch, one block per
                                range of this many histories of one instance,
                                that instance's tables in shared memory     */
@@ -75,6 +78,9 @@ public:
     /* Build tables for one problem; returns the instance index, or -1. */
     int add_instance(const nraps_problem& p, const EvBuffers& b, std::string& err);
     void clear_instances();
+    /* Allocate later instances' tables stream-ordered from `pool` on `s`
+       (the request server admits and retires instances every step). */
+    void set_pool(cudaMemPool_t pool, cudaStream_t s);
     /* Drop one instance (later instances shift down by one). */
     void remove_instance(uint32_t idx);
     uint32_t n_instances() const;

@@ -104,6 +104,12 @@ struct nraps_batch {
     uint64_t graph_kernels = 0;
     std::vector<cudaEvent_t> ev_pairs;
     double ms = 0.0;
+    /* autotuning over the first inactive generations: {block, range} */
+    std::vector<std::pair<uint32_t, uint32_t>> tune_cand;
+    std::vector<float> tune_ms;
+    std::vector<double> tune_score;
+    unsigned long long tune_coll = 0;
+    bool tuned = true;
     ~nraps_batch() {
         if (gexec) cudaGraphExecDestroy(gexec);
         for (cudaEvent_t e : ev_pairs) cudaEventDestroy(e);
@@ -133,6 +139,22 @@ int nraps_batch_create(nraps_ctx* ctx, const nraps_problem* problems, uint32_t n
         b->ev.params.range = ctx->opts.range_len ? ctx->opts.range_len : 4096;
     } else if (ctx->opts.passes == 0 && b->ev.params.K != NRAPS_ONE_PASS) {
         b->ev.params.passes = 1;
+    }
+    /* with no shape given, the first inactive generations each try one
+       (block, range length) of a ranged pass -- blocks of 128, 256 and 512
+       threads, ranges of 1024..8192 histories -- and keep the one with the
+       least time per real collision; likeliest first, so short inactive
+       phases try only the head.  Results do not depend on the shape. */
+    if (ctx->opts.block_size == 0 && ctx->opts.range_len == 0 && ctx->opts.events_per_pass == 0 &&
+        ctx->opts.passes == 0) {
+        const uint32_t cand[][2] = {{128, 4096}, {256, 4096}, {512, 4096}, {128, 2048}, {256, 8192},
+                                    {512, 8192}, {128, 8192}, {256, 2048}, {512, 2048}, {128, 1024},
+                                    {256, 1024}, {512, 1024}};
+        uint64_t skip = ~0ULL;
+        for (uint32_t i = 0; i < n; ++i) skip = std::min<uint64_t>(skip, problems[i].variables.skip);
+        const size_t budget = (size_t)std::min<uint64_t>(skip, sizeof(cand) / sizeof(cand[0]));
+        for (size_t i = 0; i < budget; ++i) b->tune_cand.emplace_back(cand[i][0], cand[i][1]);
+        b->tuned = b->tune_cand.size() < 2;
     }
     bool bank = ctx->opts.mode == NRAPS_MODE_BANK;
     for (uint32_t i = 0; i < n; ++i) {
@@ -165,6 +187,42 @@ int nraps_batch_run(nraps_batch* b, uint64_t n) {
     cudaStream_t sm = ctx->stream;
     if (b->enqueued + n > b->max_gens) n = b->max_gens - b->enqueued;
     for (uint64_t i = 0; i < n; ++i) {
+        if (!b->tuned) {
+            /* one candidate per generation, timed synchronously */
+            const size_t c = b->tune_ms.size();
+            b->ev.params.block = b->tune_cand[c].first;
+            b->ev.params.range = b->tune_cand[c].second;
+            if (b->ev.size_grid()) return set_err(ctx, NRAPS_ERR_NOMEM, "batch: ranged launch buffers");
+            cudaEvent_t e0, e1;
+            CK(cudaEventCreate(&e0)); CK(cudaEventCreate(&e1));
+            CK(cudaEventRecord(e0, sm));
+            int r = b->ev.enqueue_generation(sm);
+            if (r < 0) return set_err(ctx, NRAPS_ERR_CUDA, std::string("kernel launch failed: ") + cudaGetErrorString(cudaGetLastError()));
+            ctx->launches += (uint64_t)r;
+            CK(cudaEventRecord(e1, sm));
+            CK(cudaEventSynchronize(e1));
+            float ms = 0.f;
+            CK(cudaEventElapsedTime(&ms, e0, e1));
+            cudaEventDestroy(e0); cudaEventDestroy(e1);
+            GenState g;
+            CK(cudaMemcpy(&g, b->ev.n_instances() == 1 ? b->buf[0]->st : b->ev.batch_stats(), sizeof g,
+                          cudaMemcpyDeviceToHost));
+            const unsigned long long coll = g.tot_collisions - b->tune_coll;
+            b->tune_coll = g.tot_collisions;
+            b->tune_ms.push_back(ms);
+            b->tune_score.push_back(coll ? (double)ms / (double)coll : (double)ms);
+            b->ms += ms;
+            if (b->tune_ms.size() == b->tune_cand.size()) {
+                size_t best = 0;
+                for (size_t j = 1; j < b->tune_score.size(); ++j) if (b->tune_score[j] < b->tune_score[best]) best = j;
+                b->ev.params.block = b->tune_cand[best].first;
+                b->ev.params.range = b->tune_cand[best].second;
+                if (b->ev.size_grid()) return set_err(ctx, NRAPS_ERR_NOMEM, "batch: ranged launch buffers");
+                b->tuned = true;
+            }
+            b->enqueued++;
+            continue;
+        }
         cudaEvent_t e0, e1;
         CK(cudaEventCreate(&e0)); CK(cudaEventCreate(&e1));
         CK(cudaEventRecord(e0, sm));
@@ -228,6 +286,16 @@ int nraps_batch_results(nraps_batch* b, uint32_t i, nraps_result* out) {
                                 out);
 }
 
+int nraps_batch_tuning(nraps_batch* b, uint32_t* block, uint32_t* range_len, uint32_t* n_tried, float* tried_ms,
+                       uint32_t tried_cap) {
+    if (!b) return NRAPS_ERR_INVALID;
+    if (block) *block = b->ev.params.block;
+    if (range_len) *range_len = b->ev.params.range;
+    if (n_tried) *n_tried = (uint32_t)b->tune_ms.size();
+    for (uint32_t i = 0; tried_ms && i < tried_cap && i < b->tune_ms.size(); ++i) tried_ms[i] = b->tune_ms[i];
+    return NRAPS_OK;
+}
+
 int nraps_batch_timing(nraps_batch* b, double* ms, uint64_t* histories, uint64_t* collisions) {
     if (!b) return NRAPS_ERR_INVALID;
     int st = nraps_batch_sync(b);
@@ -274,6 +342,9 @@ struct Request {
 double now_s(const std::chrono::steady_clock::time_point& t0) {
     return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
 }
+
+/* most generations one server step runs without a host round trip */
+constexpr uint64_t SERVER_MAX_STEP_GENERATIONS = 4;
 
 }  // namespace
 
@@ -326,6 +397,11 @@ int nraps_server_create(nraps_ctx* ctx, const nraps_server_opts* opts, nraps_ser
     } else if (ctx->opts.passes == 0 && s->ev.params.K != NRAPS_ONE_PASS) {
         s->ev.params.passes = 1;
     }
+    /* admitted requests' buffers and tables come from the context's
+       stream-ordered pool: admissions and retirements then neither call
+       cudaMalloc/cudaFree nor synchronise the device */
+    cudaMemPool_t pool = nrint::ctx_pool(ctx);
+    if (pool) s->ev.set_pool(pool, ctx->stream);
     CK(s->states.alloc((size_t)s->o.max_slots * sizeof(GenState)));
     for (uint32_t i = s->o.max_slots; i > 0; --i) s->free_slots.push_back(i - 1);
     s->host_states.resize(s->o.max_slots);
@@ -382,7 +458,7 @@ int nraps_server_step(nraps_server* s, uint32_t* n_running, uint32_t* n_finished
         GenState* slot_state = s->states.as<GenState>() + r.slot;
         cudaError_t e = r.buf->alloc(p.variables.energygroups, p.mesh.n_cells, p.variables.generations,
                                      p.variables.histories, ctx->opts.bank_factor, bank, (double)p.k_new,
-                                     slot_state, sm);
+                                     slot_state, sm, nrint::ctx_pool(ctx));
         if (e != cudaSuccess) {
             r.state = NRAPS_REQ_DONE; r.status = nrint::cuda_status(e); r.t_done = now_s(s->t0);
             s->free_slots.push_back(r.slot);
@@ -408,12 +484,28 @@ int nraps_server_step(nraps_server* s, uint32_t* n_running, uint32_t* n_finished
         if (st) return set_err(ctx, st, err);
         s->dirty = false;
     }
+    /* generations this step: as many as no running request could retire
+       within (a request needs max(2, min_active) active generations before
+       its k can count as converged, and stops at its generation cap), at
+       most SERVER_MAX_STEP_GENERATIONS -- young requests then cost one host
+       round trip per few generations instead of one per generation */
+    uint64_t ng = SERVER_MAX_STEP_GENERATIONS;
+    for (uint64_t id : s->running) {
+        const Request& q = *s->reqs[id];
+        const nraps_variables& v = q.prob.p.variables;
+        const uint64_t first_retire = v.skip + std::max<uint32_t>(2, s->o.min_active);
+        uint64_t room = first_retire > q.gens_run ? first_retire - q.gens_run : 1;
+        room = std::min<uint64_t>(room, v.generations > q.gens_run ? v.generations - q.gens_run : 1);
+        ng = std::min<uint64_t>(ng, std::max<uint64_t>(1, room));
+    }
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0)); CK(cudaEventCreate(&e1));
     CK(cudaEventRecord(e0, sm));
-    int r = s->ev.enqueue_generation(sm);
-    if (r < 0) { cudaEventDestroy(e0); cudaEventDestroy(e1); return set_err(ctx, NRAPS_ERR_CUDA, std::string("kernel launch failed: ") + cudaGetErrorString(cudaGetLastError())); }
-    ctx->launches += (uint64_t)r;
+    for (uint64_t j = 0; j < ng; ++j) {
+        int r = s->ev.enqueue_generation(sm);
+        if (r < 0) { cudaEventDestroy(e0); cudaEventDestroy(e1); return set_err(ctx, NRAPS_ERR_CUDA, std::string("kernel launch failed: ") + cudaGetErrorString(cudaGetLastError())); }
+        ctx->launches += (uint64_t)r;
+    }
     CK(cudaEventRecord(e1, sm));
     /* only the slots up to the highest one in use (slots are handed out
        lowest first) */
@@ -432,8 +524,8 @@ int nraps_server_step(nraps_server* s, uint32_t* n_running, uint32_t* n_finished
     for (size_t i = 0; i < s->running.size();) {
         Request& q = *s->reqs[s->running[i]];
         const GenState& g = s->host_states[q.slot];
+        s->histories += (g.gen - std::min<uint64_t>(q.gens_run, g.gen)) * q.prob.p.variables.histories;
         q.gens_run = g.gen;
-        s->histories += q.prob.p.variables.histories;
         uint64_t na = g.nactive;
         if (na) {
             q.k_mean = g.ksum / (double)na;

@@ -13,6 +13,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <limits>
 
 namespace {
 size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -130,6 +131,14 @@ int build_event_tables(const nraps_problem& p, EvHostTables& t, std::string& err
             }
             for (uint64_t e = 0; e < G; ++e) t.scdf[(m * G + g) * G + e] = (c > 0.f) ? cum[e] / c : 1.f;
         }
+    /* one uniform decides absorption and the scatter group together */
+    t.ocdf.assign(M * G * G, 1.f);
+    for (uint64_t j = 0; j < M * G; ++j) {
+        const float pa = t.xs[j * 4 + 1];
+        const float q = 1.0f - pa;
+        t.ocdf[j * G] = pa;
+        for (uint64_t e = 1; e < G; ++e) t.ocdf[j * G + e] = pa + q * t.scdf[j * G + e - 1];
+    }
     t.chicdf.assign(M * G, 0.f);
     for (uint64_t m = 0; m < M; ++m) {
         float c = 0.f;
@@ -176,17 +185,46 @@ int build_event_tables(const nraps_problem& p, EvHostTables& t, std::string& err
         if (!(w > 0.0)) { err = "material region of zero width"; return 1; }
         wmin = std::min(wmin, w);
     }
-    uint64_t want = (uint64_t)std::ceil(4.0 * (double)t.L / wmin);
+    /* bins no wider than half the narrowest region: at most one region
+       boundary per bin, unless the 16384-bin cap binds */
+    uint64_t want = (uint64_t)std::ceil(2.0 * (double)t.L / wmin);
     uint32_t nb = 16;
     while (nb < want && nb < 16384) nb <<= 1;
     t.nbins = nb;
     t.inv_binw = (float)((double)nb / (double)t.L);
-    t.grid.assign(nb, 0);
-    uint32_t r = 0;
+    /* The device maps x to bin (int)(x * inv_binw) (one f32 multiply,
+       truncation, clamp to [0, nb-1]); that map never decreases with x.  So
+       every x >= boundary B lies in a bin >= bin(B), and every x in a bin
+       > bin(B) is >= B: the first region a bin can hold is the number of
+       boundaries whose own bin lies below it. */
+    auto bin_of = [&](float xv) -> uint32_t {
+        float f = xv * t.inv_binw;
+        int b = (int)f;
+        b = b < 0 ? 0 : (b >= (int)nb ? (int)nb - 1 : b);
+        return (uint32_t)b;
+    };
+    std::vector<uint32_t> first_region(nb, 0), boundaries(nb, 0);
+    for (uint32_t r = 1; r < t.R; ++r) boundaries[bin_of(t.rleft[r])]++;
+    uint32_t below = 0;
+    for (uint32_t b = 0; b < nb; ++b) { first_region[b] = below; below += boundaries[b]; }
+    t.bins.assign(2 * (size_t)nb, 0);
     for (uint32_t b = 0; b < nb; ++b) {
-        double xb = (double)b * (double)t.L / (double)nb;
-        while (r + 1 < t.R && (double)t.rleft[r + 1] <= xb) ++r;
-        t.grid[b] = (uint16_t)r;
+        const uint32_t r0 = first_region[b];
+        const float x1 = r0 + 1 < t.R ? t.rleft[r0 + 1] : std::numeric_limits<float>::infinity();
+        uint32_t xb;
+        std::memcpy(&xb, &x1, 4);
+        t.bins[2 * b] = xb;
+        t.bins[2 * b + 1] = r0 | (boundaries[b] > 1 ? 0x80000000u : 0u);
+    }
+    t.rdat.assign(4 * ((size_t)t.R + 1), 0.f);
+    for (uint32_t r = 0; r <= t.R; ++r) {
+        float* d = &t.rdat[4 * (size_t)r];
+        d[0] = t.rleft[r];
+        if (r < t.R) {
+            d[1] = t.rinvdx[r];
+            std::memcpy(&d[2], &t.rfirst[r], 4);
+            std::memcpy(&d[3], &t.rncell[r], 4);
+        }
     }
     t.fuel.resize(p.n_fuel);
     for (uint64_t i = 0; i < p.n_fuel; ++i) {

@@ -20,16 +20,28 @@ struct TableLayout {
    (bitwise) width, so a cell index inside a region is arithmetic.
      sigtr  = f32(sigt - mu*sigs) evaluated in FP64 (exact product)
      pabs   = siga / sigtr,  nsf_st = (nut*sigf) / sigtr,  inv_st = 1 / sigtr
-     scdf   = transport-corrected scatter CDF (within-group term minus mu*sigs)
+     ocdf   = outcome CDF of a real collision, G entries per (m, g): entry 0 is
+              pabs (absorbed), entry e >= 1 is pabs + (1 - pabs) * scdf[e-1]
+              (scattered into a group below e), scdf being the
+              transport-corrected scatter CDF (within-group term minus
+              mu*sigs); one uniform u picks the outcome: absorbed if
+              u < ocdf[0], else group (number of entries <= u) - 1
      maj[g] = max of sigtr over the materials present, maj[G+g] = 1/maj[g]
-     grid   = first region of each of nbins equal bins of [0, L]             */
+     rdat   = per region (R+1 entries, the last holds left = L): left edge,
+              1/cell width, first cell, cells (the last two as u32 bits)
+     bins   = nbins equal bins of [0, L]; bin b holds the first region r0 any
+              x with (int)(x * inv_binw) == b can lie in, the next region's
+              left edge x1 (r = r0 + (x >= x1)), and bit 31 of the region
+              word set when the bin holds more than one region boundary
+              (then the lookup walks on)                                    */
 struct EvHostTables {
     uint32_t M = 0, G = 0, R = 0, nc = 0, nbins = 0, nfuel = 0;
     float L = 0.f, inv_binw = 0.f, boundl = 0.f, boundr = 0.f;
-    std::vector<float> xs, scdf, chicdf, maj, rleft, rinvdx, cleft, cdx;
+    std::vector<float> xs, scdf, ocdf, chicdf, maj, rleft, rinvdx, cleft, cdx;
+    std::vector<float> rdat;            /* 4 per region, R+1 regions            */
     std::vector<uint8_t> rmat, cmat;
     std::vector<uint32_t> rfirst, rncell, fuel;
-    std::vector<uint16_t> grid;
+    std::vector<uint32_t> bins;         /* 2 per bin: x1 bits, r0 | multi << 31 */
     std::vector<double> nsf64, dx64, inv_dx64;
     std::vector<double> inv_st64;       /* [m*G+g] (double)(1/sigtr): flux score  */
     std::vector<uint64_t> kq;           /* [m*G+g] nsf_st in 2^-32 fixed point    */

@@ -368,7 +368,7 @@ static void run_generation(const Tab<T>& t, const nraps_opts& o, uint64_t gen, d
 struct WTab {
     uint32_t M, G, R, nc, nfuel;
     float L, boundl, boundr;
-    std::vector<float> sigtr, pabs, nsf_st, inv_st, scdf, chicdf, maj, inv_maj;
+    std::vector<float> sigtr, pabs, nsf_st, inv_st, scdf, ocdf, chicdf, maj, inv_maj;
     std::vector<float> rleft, rinvdx, cleft, cdx;
     std::vector<uint8_t> rmat, cmat;
     std::vector<uint32_t> rfirst, rncell, fuel;
@@ -403,6 +403,14 @@ static WTab make_wtab(const nraps_problem& p) {
             }
             for (uint32_t e = 0; e < G; ++e) t.scdf[(m * G + g) * G + e] = c > 0.0f ? cum[e] / c : 1.0f;
         }
+    /* outcome CDF of a real collision: absorbed below pabs, else scattered
+       into the group whose share of the remaining 1 - pabs the uniform hits */
+    t.ocdf.assign(M * G * G, 1.0f);
+    for (uint32_t j = 0; j < M * G; ++j) {
+        const float q = 1.0f - t.pabs[j];
+        t.ocdf[j * G] = t.pabs[j];
+        for (uint32_t e = 1; e < G; ++e) t.ocdf[j * G + e] = t.pabs[j] + q * t.scdf[j * G + e - 1];
+    }
     t.chicdf.resize(M * G);
     for (uint32_t m = 0; m < M; ++m) {
         float c = 0.0f;
@@ -461,8 +469,12 @@ static void woodcock_history(const WTab& t, Pcg32& rng, double* tally, uint64_t&
         mu = 2.0f * w_u24(rng) - 1.0f;
         g = w_chi(&t.chicdf[t.cmat[cell] * G], G, w_u24(rng));
     } else {
-        x = src->x; g = src->group;
+        /* a fission neutron draws its group at birth from chi of the material
+           of the cell it was born in (the site carries no group) */
+        x = src->x;
         mu = 2.0f * w_u24(rng) - 1.0f;
+        const uint32_t c = src->cell < t.nc ? src->cell : t.nc - 1;
+        g = w_chi(&t.chicdf[t.cmat[c] * G], G, w_u24(rng));
     }
     uint64_t events = 0;
     uint32_t seq = 0, last_cell = 0;
@@ -507,16 +519,17 @@ static void woodcock_history(const WTab& t, Pcg32& rng, double* tally, uint64_t&
             int n = (int)std::floor(nu);
             if (n > 64) n = 64;
             for (int i = 0; i < n; ++i) {
-                uint32_t sg = w_chi(&t.chicdf[m * G], G, w_u24(rng));
-                if (sites) sites->push_back(SiteU{x, cell, sg, hid, seq});
+                if (sites) sites->push_back(SiteU{x, cell, 0u, hid, seq});
                 ++seq;
             }
         }
-        if (w_u24(rng) < t.pabs[j]) { fate = NRAPS_FATE_ABSORBED; break; }
-        float xi = w_u24(rng);
-        uint32_t ng = G - 1;
-        for (uint32_t e = 0; e + 1 < G; ++e) if (xi < t.scdf[j * G + e]) { ng = e; break; }
-        g = ng;
+        /* one uniform: absorbed if below ocdf[0], else the scatter group is
+           the number of outcome-CDF entries at or below it, minus one */
+        const float u = w_u24(rng);
+        uint32_t o = 0;
+        for (uint32_t e = 0; e < G; ++e) o += (t.ocdf[j * G + e] <= u) ? 1u : 0u;
+        if (o == 0) { fate = NRAPS_FATE_ABSORBED; break; }
+        g = o - 1;
         mu = 2.0f * w_u24(rng) - 1.0f;
     }
     rec.fate = fate; rec.final_group = g; rec.final_x = (double)x; rec.final_cell = last_cell;

@@ -176,3 +176,24 @@ def test_server_finished_ids(ctx_factory):
         st, info, _ = srv.poll(rid, results=False)
         assert st == abi.OK and info["generations_run"] >= 2
     srv.close()
+
+
+def test_batch_autotuner_tries_shapes_without_changing_results(ctx_factory):
+    """A batch given no launch shape tries blocks of 128/256/512 threads with
+    ranges of 1024..8192 histories over its first inactive generations; every
+    instance's k sequence equals that of the same batch run at one fixed
+    shape, and the choice is one of the candidates."""
+    probs = instances(5, seed=13, inactive=12, active=4)
+    seeds = [900 + i for i in range(len(probs))]
+    tuned = api.Batch(ctx_factory(seed=1, **WC), probs, seeds=seeds)
+    tuned.run(probs[0].generations)
+    t = tuned.tuning()
+    fixed = api.Batch(ctx_factory(seed=1, block_size=512, range_len=2048, **WC), probs, seeds=seeds)
+    fixed.run(probs[0].generations)
+    assert len(t["tried_ms"]) == 12 and min(t["tried_ms"]) > 0
+    assert t["block"] in (128, 256, 512) and t["range_len"] in (1024, 2048, 4096, 8192)
+    assert fixed.tuning()["tried_ms"] == [] and fixed.tuning()["block"] == 512
+    for i in range(len(probs)):
+        assert np.array_equal(tuned.results(i).k64, fixed.results(i).k64), i
+    tuned.close()
+    fixed.close()

@@ -70,14 +70,14 @@ def test_event_reflective_bitexact(ctx_factory):
     assert gkq == wkq and np.all(grec["fate"] != abi.FATE_LEAKED)
 
 
-# pool transport: particles in shared memory, block-wide phases (one instance)
-POOL_SHAPES = [dict(pool_slots=64), dict(pool_slots=1024), dict(range_len=64), dict(range_len=1024)]
+# sorted transport (event-type queues, one instance) and ranged launches
+SORT_SHAPES = [dict(sort_rounds=1), dict(sort_rounds=8), dict(range_len=64), dict(range_len=1024)]
 
 
 def test_event_results_independent_of_queue_shape(ctx_factory):
     p = small(hist=20000, gens=10, skip=3)
     ks = []
-    for shape in SHAPES + POOL_SHAPES:
+    for shape in SHAPES + SORT_SHAPES:
         r = ctx_factory(seed=7, mode=abi.MODE_BANK, precision=abi.PREC_FP32,
                         tracking=abi.TRACK_WOODCOCK, **shape).solve(p)
         ks.append(r.k64)
@@ -162,36 +162,38 @@ def test_autotuner_leaves_results_unchanged(ctx_factory):
     s.close()
     fixed = ctx_factory(events_per_pass=4, passes=3, block_size=256, **base).solve(p)
     assert np.array_equal(r.k64, fixed.k64)
-    assert len(t["tried_ms"]) == 10 and min(t["tried_ms"]) > 0
+    assert len(t["tried_ms"]) == 12 and min(t["tried_ms"]) > 0
     assert t["block"] in (128, 256) and t["events_per_pass"] >= 1
     # one-pass shapes run every particle to its end (no queue passes)
     assert t["passes"] >= 1 or t["events_per_pass"] == abi.ONE_PASS
 
 
 @pytest.mark.parametrize("mode", [abi.MODE_PHYSICS, abi.MODE_BANK])
-def test_pool_transport_exact_log_matches(ctx_factory, mode):
-    """The pool transport against the warp transport with the shared
-    software logarithm: every history identical, so k, tallies and bank
-    order (entropy) agree exactly, and the sessions report one transport
-    launch per generation."""
+def test_sorted_transport_exact_log_matches(ctx_factory, mode):
+    """The sorted transport (flight and collision kernels over event-type
+    queues, then one pass for the survivors) against the warp transport with
+    the shared software logarithm: every history identical, so k, tallies and
+    bank order (entropy) agree exactly; 2R+1 transport launches per
+    generation."""
     p = small(hist=7000, gens=8, skip=3)
     base = dict(seed=77, mode=mode, precision=abi.PREC_FP32, tracking=abi.TRACK_WOODCOCK, exact_log=1)
     warp = ctx_factory(block_size=128, events_per_pass=abi.ONE_PASS, passes=0, **base).solve(p)
-    for slots in (64, 512, 4096):
-        pool = ctx_factory(pool_slots=slots, **base).solve(p)
-        assert np.array_equal(pool.k64, warp.k64), slots
-        np.testing.assert_allclose(pool.flux_mean, warp.flux_mean, rtol=1e-12, atol=0)
-        np.testing.assert_allclose(pool.entropy, warp.entropy, rtol=0, atol=1e-12)
-        assert pool.stats.collisions == warp.stats.collisions
-        assert pool.stats.transport_launches == p.generations
+    for rounds in (1, 4, 16):
+        srt = ctx_factory(sort_rounds=rounds, **base).solve(p)
+        assert np.array_equal(srt.k64, warp.k64), rounds
+        np.testing.assert_allclose(srt.flux_mean, warp.flux_mean, rtol=1e-12, atol=0)
+        np.testing.assert_allclose(srt.entropy, warp.entropy, rtol=0, atol=1e-12)
+        assert srt.stats.collisions == warp.stats.collisions
+        assert srt.stats.virtual_collisions == warp.stats.virtual_collisions
+        assert srt.stats.transport_launches == p.generations * (2 * rounds + 1)
 
 
-def test_pool_slots_validated(ctx_factory):
+def test_sort_rounds_validated(ctx_factory):
     p = small(hist=1000, gens=3, skip=1)
-    for bad in (1, 5000):
-        with pytest.raises(api.NrapsError):
-            ctx_factory(seed=1, mode=abi.MODE_BANK, precision=abi.PREC_FP32, tracking=abi.TRACK_WOODCOCK,
-                        pool_slots=bad).solve(p)
+    with pytest.raises(api.NrapsError) as e:
+        ctx_factory(seed=1, mode=abi.MODE_BANK, precision=abi.PREC_FP32, tracking=abi.TRACK_WOODCOCK,
+                    sort_rounds=17).solve(p)
+    assert e.value.status == abi.ERR_INVALID
 
 
 @pytest.mark.parametrize("tracking", [abi.TRACK_WOODCOCK, abi.TRACK_SURFACE])
@@ -232,3 +234,22 @@ def test_ranged_launch_exact_log_matches(ctx_factory, mode):
     with pytest.raises(api.NrapsError) as e:
         ctx_factory(range_len=32769, **base).solve(p)
     assert e.value.status == abi.ERR_INVALID
+
+
+def test_tuner_choice_cached_per_shape(ctx_factory):
+    """A second session of the same problem shape on one context starts with
+    the first session's choice and tries nothing; results are unchanged."""
+    p = small(hist=20000, gens=14, skip=12)
+    ctx = ctx_factory(seed=23, mode=abi.MODE_BANK, precision=abi.PREC_FP32, tracking=abi.TRACK_WOODCOCK)
+    s1 = ctx.session(p)
+    s1.run(p.generations)
+    r1, t1 = s1.results(), s1.tuning()
+    s1.close()
+    s2 = ctx.session(p)
+    s2.run(p.generations)
+    r2, t2 = s2.results(), s2.tuning()
+    s2.close()
+    assert len(t1["tried_ms"]) == 12 and len(t2["tried_ms"]) == 0
+    for key in ("block", "events_per_pass", "passes", "tail_lanes", "sort_rounds", "range_len"):
+        assert t1[key] == t2[key], key
+    assert np.array_equal(r1.k64, r2.k64)
