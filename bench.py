@@ -247,41 +247,46 @@ def measure_e2e(prob, arm: str, seed: int, device: int):
            + r.k64.nbytes + r.entropy.nbytes + r.flux_mean.nbytes + r.flux_sem.nbytes)
     g = prob.generations
     return dict(value=prob.histories * g / dt, seconds=dt, h2d=h2d / g, d2h=d2h / g, k_mean=r.stats.k_mean,
-                k_sigma=r.stats.k_sigma, generations=g)
+                k_sigma=r.stats.k_sigma, generations=g, k64=r.k64.copy())
 
 
-def measure_parity(full, seed: int, device: int, plain_active: int = 100, event_batch: int = 20,
-                   plain_batch: int = 10, plain_ms_per_generation: float | None = None,
-                   event_ms_per_generation: float | None = None, coarse: int = 1):
+def measure_parity(full, seed: int, device: int, replicas: int = 6, inactive: int = 20, active: int = 30,
+                   plain_ms_per_generation: float | None = None, event_ms_per_generation: float | None = None,
+                   event_k64=None, coarse=(1, 100)):
     """The chosen form (event Woodcock, FP32 flights) against the plain FP64
-    kernel on the same workload and seeds, BANK mode both: k difference with
-    a batch-means sigma, per-group flux chi^2 and integrated-flux bias, and
-    the wall time each form needs to reach sigma_k <= 50 pcm."""
+    kernel on the same workload (geometry, cross sections, histories per
+    generation), BANK mode both, from `replicas` independent seeds each
+    (inactive + active generations per replica): k difference with its
+    combined error, per-group flux chi^2 (per cell and over 100-cell bins)
+    and the group's integrated-flux bias; the wall time each form needs to
+    reach sigma_k <= 50 pcm."""
     from nraps_gb300 import api, parity
-    runs = {}
-    for arm, active, batch in (("event", full.generations - full.skip, event_batch),
-                               ("plain", plain_active, plain_batch)):
-        p = full.with_(generations=full.skip + active)
-        ctx = api.Context(seed=seed, device=device, **ARMS[arm])
-        s = ctx.session(p)
-        runs[arm] = parity.run_batches(s, p, batch)
-        runs[arm]["generations"] = p.generations
-        s.close()
-        ctx.close()
-    G, nc, skip = full.energygroups, full.n_cells, full.skip
-    c = parity.compare(runs["event"], runs["plain"], G, nc, skip, coarse=coarse)
-    c["workload"] = full.name.split(":")[0]
-    c["event"] = {"generations": f"{skip} + {runs['event']['generations'] - skip}",
-                  "batch": event_batch, "k_mean": c.pop("k_a"), "sigma_pcm": c.pop("sigma_a_pcm")}
-    c["plain_fp64"] = {"generations": f"{skip} + {runs['plain']['generations'] - skip}",
-                       "batch": plain_batch, "k_mean": c.pop("k_b"), "sigma_pcm": c.pop("sigma_b_pcm")}
-    for arm, key, ms in (("event", "event", event_ms_per_generation),
-                         ("plain", "plain_fp64", plain_ms_per_generation)):
-        if ms:
-            c[key]["time_to_50pcm"] = parity.time_to_sigma(runs[arm]["k64"][skip:], ms, skip)
-    c["same_seeds"] = True
-    c["mode"] = "BANK"
-    return c
+    p = full.with_(generations=inactive + active, skip=inactive)
+    seeds = [seed * 7919 + 13 * i for i in range(replicas)]
+
+    def make(**kw):
+        return api.Context(device=device, **kw)
+
+    ev = parity.run_replicas(make, p, seeds, **ARMS["event"])
+    pl = parity.run_replicas(make, p, seeds, **ARMS["plain"])
+    G, nc = full.energygroups, full.n_cells
+    out = {"workload": full.name.split(":")[0], "mode": "BANK", "same_seeds": True,
+           "replicas": replicas, "generations_per_replica": f"{inactive} + {active}"}
+    for cz in coarse:
+        c = parity.compare_replicas(ev, pl, G, nc, coarse=cz)
+        if cz == coarse[0]:
+            out.update({k: c[k] for k in ("k_a", "k_b", "sigma_a_pcm", "sigma_b_pcm", "delta_k_pcm",
+                                          "sigma_pcm", "z")})
+            out["k_event"], out["k_plain_fp64"] = out.pop("k_a"), out.pop("k_b")
+            out["sigma_event_pcm"], out["sigma_plain_fp64_pcm"] = out.pop("sigma_a_pcm"), out.pop("sigma_b_pcm")
+        out[f"flux_{cz}_cells_per_bin"] = c["flux"]
+    if event_k64 is not None and event_ms_per_generation:
+        out["event_time_to_50pcm"] = parity.time_to_sigma(event_k64[full.skip:], event_ms_per_generation,
+                                                          full.skip)
+    if plain_ms_per_generation:
+        out["plain_fp64_time_to_50pcm"] = parity.time_to_sigma(pl["k64"][0][inactive:], plain_ms_per_generation,
+                                                               inactive)
+    return out
 
 
 def measure_plain_small(seed: int, device: int, threads: int):
@@ -300,10 +305,15 @@ def measure_plain_small(seed: int, device: int, threads: int):
     r = O.monte_carlo(p, o, threads=threads, acc64=False)
     dt = time.perf_counter() - t
     k = r.k64[skip:]
+    # COMPAT keeps the reference's 0/0 at a zero cosine (src/mc_code.rs:184):
+    # a generation that drew mu == 0 exactly has a NaN k
+    ok = np.isfinite(k)
     out["cpu_port_compat_f32"] = {
         "histories_per_s": (p.histories + threads) * p.generations / dt, "seconds": dt, "cores": threads,
-        "k_mean": float(k.mean()), "sigma_pcm": parity.naive_sigma(k) * 1e5,
-        "time_to_50pcm": parity.time_to_sigma(k, 1000.0 * dt / p.generations, skip)}
+        "k_mean": float(k[ok].mean()) if ok.any() else None,
+        "sigma_pcm": parity.naive_sigma(k[ok]) * 1e5 if ok.sum() > 1 else None,
+        "nan_generations": int((~ok).sum()),
+        "time_to_50pcm": parity.time_to_sigma(k[ok], 1000.0 * dt / p.generations, skip)}
     for name, mode in (("gpu_plain_fp64_compat", abi.MODE_COMPAT), ("gpu_plain_fp64_bank", abi.MODE_BANK)):
         ctx = api.Context(seed=12345, device=device, mode=mode, precision=abi.PREC_FP64,
                           compat_threads=threads if mode == abi.MODE_COMPAT else 0)
@@ -316,11 +326,16 @@ def measure_plain_small(seed: int, device: int, threads: int):
         s.close()
         ctx.close()
         k = res.k64[skip:]
+        ok = np.isfinite(k)
         ms_gen = tm["total_ms"] / p.generations
         hist = (p.histories + (threads if mode == abi.MODE_COMPAT else 0)) * p.generations
         out[name] = {"histories_per_s": hist / (tm["total_ms"] / 1000.0), "ms_per_generation": ms_gen,
-                     "k_mean": float(k.mean()), "sigma_pcm": parity.naive_sigma(k) * 1e5,
-                     "time_to_50pcm": parity.time_to_sigma(k, ms_gen, skip)}
+                     "k_mean": float(k[ok].mean()) if ok.any() else None,
+                     "sigma_pcm": parity.naive_sigma(k[ok]) * 1e5 if ok.sum() > 1 else None,
+                     "nan_generations": int((~ok).sum()),
+                     "time_to_50pcm": parity.time_to_sigma(k[ok], ms_gen, skip)}
+    out["note"] = ("10k histories per generation: sigma_k per generation is ~1100 pcm, so 100 active "
+                   "generations reach ~110 pcm, not 50")
     return out
 
 
@@ -330,10 +345,14 @@ def measure_batched(seed: int, device: int, steps: int, warmup: int = 3):
     CUDA-graph replay per generation."""
     import torch
     from nraps_gb300 import api, synth
+    # the batch's autotuner tries 12 launch shapes over its first inactive
+    # generations: warm up past them so the timed generations run the choice
+    warmup = max(warmup, 14)
     probs = synth.batched(seed, n=256, inactive=max(20, warmup), active=max(20, steps))
     ctx = api.Context(seed=seed, device=device, use_graphs=1, **ARMS["event"])
     b = api.Batch(ctx, probs, seeds=[seed * 1000 + i for i in range(len(probs))])
     b.run(warmup)
+    tuning = b.tuning()
     t0 = b.timing()
     launches0 = ctx.launches
     b.run(steps)
@@ -344,7 +363,9 @@ def measure_batched(seed: int, device: int, steps: int, warmup: int = 3):
            "steps": steps, "ms_per_step": ms / steps, "histories_per_s": hist / (ms / 1000.0),
            "collisions_per_s": (t1["collisions"] - t0["collisions"]) / (ms / 1000.0),
            "gpu_launches": ctx.launches - launches0, "graphs": True,
-           "groups": "U{2..8}", "regions": "U{4..64}"}
+           "groups": "U{2..8}", "regions": "U{4..64}",
+           "launch_shape": {"block": tuning["block"], "range_len": tuning["range_len"],
+                            "tried_ms": tuning["tried_ms"]}}
     b.close()
     ctx.close()
     return out
@@ -536,8 +557,10 @@ def main():
 
     full = full_workload(args.workload, args.seed)
     e2e = None
+    e2e_k64 = None
     if not args.no_e2e:
         e = measure_e2e(full, arm, seed, local)
+        e2e_k64 = e["k64"]
         e_sec = max_over_ranks(e["seconds"], f"cuda:{local}")
         e2e = {"value": replica_throughput(full.histories * full.generations, 1000.0 * e_sec, world),
                "unit": "histories/s", "h2d_bytes_per_step": e["h2d"],
@@ -548,10 +571,11 @@ def main():
     fp = None
     if arm == "event" and args.parity and rank == 0:
         fp = measure_parity(full, seed, local, event_ms_per_generation=ms / args.steps,
-                            plain_ms_per_generation=plain["ms_per_step"] if plain else None)
+                            plain_ms_per_generation=plain["ms_per_step"] if plain else None,
+                            event_k64=e2e_k64)
         if plain:
-            plain["k_mean"], plain["sigma_k_pcm"] = fp["plain_fp64"]["k_mean"], fp["plain_fp64"]["sigma_pcm"]
-            plain["k_from"] = f"fp32_vs_fp64 run ({fp['plain_fp64']['generations']} generations)"
+            plain["k_mean"], plain["sigma_k_pcm"] = fp["k_plain_fp64"], fp["sigma_plain_fp64_pcm"]
+            plain["k_from"] = f"fp32_vs_fp64 replicas ({fp['replicas']} x {fp['generations_per_replica']})"
 
     peak, peak_kind = peaks()
     per_launch_ms = d["transport_ms"] / max(1, d["transport_launches"])

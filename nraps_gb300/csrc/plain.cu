@@ -12,7 +12,11 @@
  *   flight after a scatter (:209).
  * PHYSICS/BANK carry the track length explicitly (no 0/0 at mu == 0), refresh
  * the xs index after every scatter, sample the scatter group with one draw,
- * and (BANK) bank floor(nu*sigf/sigtr/k + r) sites per collision.
+ * and (BANK) bank floor(nu*sigf/sigtr/k + r) sites per collision.  Their
+ * distance to a face is (face - x) * (1/mu), 1/mu set with mu, and a
+ * history's k score is summed by fused multiply-adds in FP64 and fixed to
+ * 2^-32 once at the history's end (the crossing loop is bound by the FP64
+ * pipe: these remove a division and a conversion per crossing).
  *
  * This translation unit is compiled with --fmad=false and -prec-div=true: the
  * results must match a CPU restatement bit for bit, so no multiply-add may be
@@ -164,7 +168,7 @@ __device__ void compat_history(const PlainArgs<T>& a, uint64_t h, uint64_t seed,
     }
 }
 
-template <class T, bool BANK>
+template <class T, bool BANK, bool REC>
 __device__ void physics_history(const PlainArgs<T>& a, uint64_t h, uint64_t seed, T inv_k,
                                 const nraps_site* src, uint64_t n_src,
                                 Counters& c, nraps_history_record* out) {
@@ -189,39 +193,42 @@ __device__ void physics_history(const PlainArgs<T>& a, uint64_t h, uint64_t seed
     nraps_history_record rec = {};
     int fate = NRAPS_FATE_ABSORBED;
     const T inf = tinf<T>();
+    /* FP64 is ~1/64 of the FP32 rate on this part and the crossing loop is
+       FP64-bound: a flight multiplies by 1/mu (set with mu) instead of
+       dividing per crossing, and the history's k score is one fused
+       multiply-add per track piece, fixed to 2^-32 once per history */
+    T inv_mu = mu != T(0) ? T(1) / mu : inf;
+    double ks = 0.0;
     for (;;) {
         rec.segments++;
-        uint64_t xs = __ldg(&a.mat[cell]) + (uint64_t)M * g;
+        const uint8_t m = __ldg(&a.mat[cell]);      /* fixed within the segment */
+        uint64_t xs = m + (uint64_t)M * g;
+        double nsf = (double)__ldg(&a.nsf[xs]);
         T l = -lg(upos<T>(rng.next())) * __ldg(&a.inv_sigtr[xs]);
         bool stop = false, same = true;
         while (same) {
             if (++events > a.max_events) { fate = NRAPS_FATE_CAPPED; stop = true; break; }
-            T face = (mu >= T(0)) ? __ldg(&a.right[cell]) : __ldg(&a.left[cell]);
-            T lf = (mu != T(0)) ? (face - x) / mu : inf;
-            uint8_t m = __ldg(&a.mat[cell]);
-            T nsf = __ldg(&a.nsf[m + (uint64_t)M * g]);
+            const bool fwd = mu >= T(0);
+            T face = fwd ? __ldg(&a.right[cell]) : __ldg(&a.left[cell]);
+            T lf = (mu != T(0)) ? (face - x) * inv_mu : inf;
             if (lf < l) {
                 atomicAdd(&a.tally[(uint64_t)g * a.nc + cell], (double)lf);
-                rec.track += (double)lf;
-                T s = nsf * lf;
-                rec.nsf_track += (double)s;
-                c.kq += nr_fix((double)s);
+                ks = __fma_rn(nsf, (double)lf, ks);
+                if (REC) rec.track += (double)lf;
                 l = l - lf; x = face;
-                if ((mu < T(0)) ? (cell == 0) : (cell == last)) {
-                    T bound = (mu >= T(0)) ? a.boundr : a.boundl;
-                    if (bound > T(0)) { mu = -mu; rec.reflections++; }
+                if (fwd ? (cell == last) : (cell == 0)) {
+                    T bound = fwd ? a.boundr : a.boundl;
+                    if (bound > T(0)) { mu = -mu; inv_mu = -inv_mu; rec.reflections++; }
                     else { fate = NRAPS_FATE_LEAKED; stop = true; break; }
                 } else {
-                    cell = (mu >= T(0)) ? cell + 1 : cell - 1;
+                    cell = fwd ? cell + 1 : cell - 1;
                     rec.crossings++;
                     if (__ldg(&a.mat[cell]) != m) same = false;
                 }
             } else {
                 atomicAdd(&a.tally[(uint64_t)g * a.nc + cell], (double)l);
-                rec.track += (double)l;
-                T s = nsf * l;
-                rec.nsf_track += (double)s;
-                c.kq += nr_fix((double)s);
+                ks = __fma_rn(nsf, (double)l, ks);
+                if (REC) rec.track += (double)l;
                 x = x + mu * l;
                 rec.collisions++;
                 if (BANK) {
@@ -241,19 +248,23 @@ __device__ void physics_history(const PlainArgs<T>& a, uint64_t h, uint64_t seed
                 for (uint32_t e = 0; e + 1 < G; ++e) if (xi < __ldg(&cdf[e])) { ng = e; break; }
                 g = ng;
                 mu = T(2) * u01<T>(rng.next()) - T(1);
+                inv_mu = mu != T(0) ? T(1) / mu : inf;
                 xs = m + (uint64_t)M * g;
+                nsf = (double)__ldg(&a.nsf[xs]);
                 l = -lg(upos<T>(rng.next())) * __ldg(&a.inv_sigtr[xs]);
             }
         }
         if (stop) break;
     }
+    c.kq += nr_fix(ks);
+    if (REC) rec.nsf_track = ks;
     c.coll += rec.collisions;
     c.cross += rec.crossings;
     if (fate == NRAPS_FATE_ABSORBED) c.absorbed++;
     else if (fate == NRAPS_FATE_LEAKED) c.leaked++;
     else c.capped++;
     if (BANK) a.sink.count[h] = seq;
-    if (out) {
+    if (REC) {
         rec.fate = fate; rec.final_cell = (uint32_t)cell; rec.final_group = g;
         rec.final_x = (double)x; rec.draws = rng.draws; rec.n_sites = seq;
         out[h] = rec;
@@ -265,7 +276,7 @@ __device__ __forceinline__ unsigned long long warp_sum(unsigned long long v) {
     return v;
 }
 
-template <class T, int MODE>
+template <class T, int MODE, bool REC>
 __global__ void __launch_bounds__(256) plain_kernel(PlainArgs<T> a) {
     const GenState* st = a.st;
     uint64_t gen = st->gen;
@@ -280,7 +291,7 @@ __global__ void __launch_bounds__(256) plain_kernel(PlainArgs<T> a) {
             const nraps_site* src = nullptr;
             uint64_t n_src = 0;
             if (MODE == NRAPS_MODE_BANK && st->n_bank > 0) { src = a.bank[gen & 1]; n_src = st->n_bank; }
-            physics_history<T, MODE == NRAPS_MODE_BANK>(a, h, seed, inv_k, src, n_src, c, a.records);
+            physics_history<T, MODE == NRAPS_MODE_BANK, REC>(a, h, seed, inv_k, src, n_src, c, a.records);
         }
     }
     unsigned long long kq = warp_sum(c.kq);
@@ -319,9 +330,16 @@ int launch_plain(const PlainArgs<T>& a, int mode, int block, cudaStream_t s) {
     if (block <= 0 || block > 256) block = 256;
     uint64_t grid = (a.n_hist + block - 1) / block;
     if (grid == 0) return 0;
-    if (mode == NRAPS_MODE_COMPAT) plain_kernel<T, NRAPS_MODE_COMPAT><<<(unsigned)grid, block, 0, s>>>(a);
-    else if (mode == NRAPS_MODE_PHYSICS) plain_kernel<T, NRAPS_MODE_PHYSICS><<<(unsigned)grid, block, 0, s>>>(a);
-    else plain_kernel<T, NRAPS_MODE_BANK><<<(unsigned)grid, block, 0, s>>>(a);
+    /* per-history records only in trace sessions (the record sums cost FP64
+       adds on every crossing) */
+    if (mode == NRAPS_MODE_COMPAT) plain_kernel<T, NRAPS_MODE_COMPAT, true><<<(unsigned)grid, block, 0, s>>>(a);
+    else if (a.records) {
+        if (mode == NRAPS_MODE_PHYSICS) plain_kernel<T, NRAPS_MODE_PHYSICS, true><<<(unsigned)grid, block, 0, s>>>(a);
+        else plain_kernel<T, NRAPS_MODE_BANK, true><<<(unsigned)grid, block, 0, s>>>(a);
+    } else {
+        if (mode == NRAPS_MODE_PHYSICS) plain_kernel<T, NRAPS_MODE_PHYSICS, false><<<(unsigned)grid, block, 0, s>>>(a);
+        else plain_kernel<T, NRAPS_MODE_BANK, false><<<(unsigned)grid, block, 0, s>>>(a);
+    }
     return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
 }
 template int launch_plain<float>(const PlainArgs<float>&, int, int, cudaStream_t);

@@ -7,13 +7,12 @@ their histories differ, so they agree in distribution only.  This module
 states that agreement for k_eff and for every group's flux:
 
 * generations of a power iteration are correlated (each one's source is the
-  previous one's bank), so standard errors come from batch means: the active
-  generations are cut into B consecutive batches, each batch's mean is one
-  sample, and the error of the mean is the spread of the batch means / sqrt(B)
-  (the batches are long enough that neighbouring batches are nearly
-  independent; the integrated autocorrelation time is reported beside it);
-* per-bin flux batch means come from snapshots of the running flux mean taken
-  between batches (``run_batches``);
+  previous one's bank), and in a slab the flux shape decorrelates slowly, so
+  the agreement statistics use independent replicas (``run_replicas``: the
+  same problem under different seeds, each replica's mean over its active
+  generations one sample); within one long run, batch means
+  (``batch_means``, ``run_batches``) give k's error and the integrated
+  autocorrelation time shows how correlated the generations are;
 * k: difference in pcm, combined sigma, z = difference / sigma;
 * flux: per group, chi^2 of the per-bin differences over the combined
   variances, its degrees of freedom and upper-tail probability, and the
@@ -145,6 +144,62 @@ def welch_z(xa, xb):
     p_half = sps.t.sf(np.abs(t[ok]), nu[ok])
     z[ok] = np.sign(t[ok]) * sps.norm.isf(np.maximum(p_half, 1e-300))
     return z
+
+
+def run_replicas(make_context, prob, seeds, **opts):
+    """Independent replicas of one solve: one context per seed (same problem,
+    options), each run to its end.  A replica's k sample is its mean k over
+    the active generations and its flux sample its per-bin mean flux, so the
+    samples are independent and their spread is an honest error whatever the
+    correlation between generations inside a replica.
+
+    Returns dict(k_samples [R], flux_samples [R, G*cells], k64 [R, gens])."""
+    ks, fl, k64 = [], [], []
+    for sd in seeds:
+        ctx = make_context(seed=int(sd), **opts)
+        try:
+            r = ctx.solve(prob)
+        finally:
+            close = getattr(ctx, "close", None)
+            if close:
+                close()
+        ks.append(float(r.k64[prob.skip:].mean()))
+        fl.append(r.flux_mean.copy())
+        k64.append(r.k64.copy())
+    return dict(k_samples=np.array(ks), flux_samples=np.stack(fl), k64=np.stack(k64))
+
+
+def compare_replicas(a: dict, b: dict, G: int, nc: int, coarse: int = 1):
+    """k and per-group flux agreement of replica sets `a` and `b`
+    (run_replicas): Welch normal scores throughout."""
+    from scipy import stats as sps
+    ka, kb = np.asarray(a["k_samples"]), np.asarray(b["k_samples"])
+    za = welch_z(ka[:, None], kb[:, None])[0]
+    sa = ka.std(ddof=1) / math.sqrt(ka.size)
+    sb = kb.std(ddof=1) / math.sqrt(kb.size)
+    out = {"k_a": float(ka.mean()), "k_b": float(kb.mean()), "sigma_a_pcm": sa * 1e5, "sigma_b_pcm": sb * 1e5,
+           "delta_k_pcm": float(ka.mean() - kb.mean()) * 1e5, "sigma_pcm": math.hypot(sa, sb) * 1e5,
+           "z": float(za), "replicas": [int(ka.size), int(kb.size)]}
+    fa = _coarse(a["flux_samples"], G, nc, coarse)
+    fb = _coarse(b["flux_samples"], G, nc, coarse)
+    groups = []
+    for g in range(G):
+        xa, xb = fa[:, g, :], fb[:, g, :]
+        z = welch_z(xa, xb)
+        ok = np.isfinite(z)
+        chi2 = float((z[ok] ** 2).sum())
+        dof = int(ok.sum())
+        ia, ib = xa.sum(1), xb.sum(1)
+        ma_i, mb_i = ia.mean(), ib.mean()
+        se = math.hypot(ia.std(ddof=1) / math.sqrt(ia.size), ib.std(ddof=1) / math.sqrt(ib.size))
+        zi = float(welch_z(ia[:, None], ib[:, None])[0])
+        groups.append({"group": g, "chi2": chi2, "dof": dof, "chi2_per_dof": chi2 / dof if dof else None,
+                       "p_value": float(sps.chi2.sf(chi2, dof)) if dof else None,
+                       "rel_diff": float(ma_i / mb_i - 1.0) if mb_i else None,
+                       "rel_sigma": float(se / mb_i) if mb_i else None, "z_integrated": zi})
+    out["flux"] = groups
+    out["coarse_cells_per_bin"] = coarse
+    return out
 
 
 def _coarse(a, G: int, nc: int, coarse: int):

@@ -262,18 +262,23 @@ static void physics_history(const Tab<T>& t, Pcg32& rng, Sink<A>& sk,
         mu = direction(uni<T>(rng));
     }
     uint64_t events = 0; uint32_t seq = 0;
+    /* the history's k score: one fused multiply-add per track piece in FP64,
+       fixed to 2^-32 once when the history ends */
+    double ks = 0.0;
     auto score = [&](T piece) {
         sk.tally[(uint64_t)g * t.nc + cell] += (A)piece;
         rec.track += (double)piece;
-        T s = t.nsf[t.mat[cell] + (uint64_t)t.M * g] * piece;
-        rec.nsf_track += (double)s;
-        sk.kq += nr_fix((double)s);
+        ks = std::fma((double)t.nsf[t.mat[cell] + (uint64_t)t.M * g], (double)piece, ks);
     };
     auto finish = [&](int fate) {
         rec.fate = fate; rec.final_cell = (uint32_t)cell; rec.final_group = g;
         rec.final_x = (double)x; rec.draws = rng.draws; rec.n_sites = seq;
+        rec.nsf_track = ks;
+        sk.kq += nr_fix(ks);
     };
     const T inf = std::numeric_limits<T>::infinity();
+    /* distances to faces multiply by 1/mu, set whenever mu is */
+    T inv_mu = mu != T(0) ? T(1) / mu : inf;
     for (;;) {
         rec.segments++;
         uint64_t xs = t.mat[cell] + (uint64_t)t.M * g;
@@ -281,13 +286,13 @@ static void physics_history(const Tab<T>& t, Pcg32& rng, Sink<A>& sk,
         for (;;) {
             if (++events > max_events) { finish(NRAPS_FATE_CAPPED); return; }
             T face = (mu >= T(0)) ? t.right[cell] : t.left[cell];
-            T lf = (mu != T(0)) ? (face - x) / mu : inf;
+            T lf = (mu != T(0)) ? (face - x) * inv_mu : inf;
             if (lf < l) {
                 score(lf);
                 l = l - lf; x = face;
                 if ((mu < T(0)) ? (cell == 0) : (cell == last)) {
                     T bound = (mu >= T(0)) ? t.boundr : t.boundl;
-                    if (bound > T(0)) { mu = -mu; rec.reflections++; }
+                    if (bound > T(0)) { mu = -mu; inv_mu = -inv_mu; rec.reflections++; }
                     else { finish(NRAPS_FATE_LEAKED); return; }
                 } else {
                     uint8_t prev = t.mat[cell];
@@ -317,6 +322,7 @@ static void physics_history(const Tab<T>& t, Pcg32& rng, Sink<A>& sk,
                 for (uint32_t e = 0; e + 1 < t.G; ++e) if (xi < cdf[e]) { ng = e; break; }
                 g = ng;
                 mu = direction(uni<T>(rng));
+                inv_mu = mu != T(0) ? T(1) / mu : inf;
                 xs = m + (uint64_t)t.M * g;
                 l = -lg(upos<T>(rng)) * t.inv_sigtr[xs];
             }

@@ -79,3 +79,44 @@ def test_time_to_sigma():
     assert parity.time_to_sigma(np.array([1.0, 2.0, 1.0]), 1.0, 0, target=1e-6) is None
     with pytest.raises(ValueError):
         parity.batch_means([1.0], 2)
+
+
+def test_replica_comparison_null_and_bias():
+    rng = np.random.default_rng(3)
+    G, nc, R = 2, 300, 8
+    base = np.tile(np.linspace(1, 2, nc), G)
+
+    def reps(k, bias):
+        return dict(k_samples=k + rng.normal(0, 1e-3, R),
+                    flux_samples=base * (1 + bias) + rng.normal(0, 0.02, (R, G * nc)))
+    c = parity.compare_replicas(reps(1.0, 0.0), reps(1.0, 0.0), G, nc, coarse=10)
+    assert abs(c["z"]) < 4 and c["replicas"] == [R, R]
+    assert all(g["dof"] == 30 and g["p_value"] > 1e-4 and abs(g["z_integrated"]) < 4 for g in c["flux"])
+    d = parity.compare_replicas(reps(1.01, 0.02), reps(1.0, 0.0), G, nc, coarse=10)
+    assert d["z"] > 5 and all(g["z_integrated"] > 5 for g in d["flux"])
+
+
+def test_run_replicas_uses_each_seed_once():
+    calls = []
+
+    class FakeResult:
+        def __init__(self, seed):
+            self.k64 = np.full(6, 1.0 + seed * 1e-4)
+            self.flux_mean = np.full(4, float(seed))
+
+    class FakeCtx:
+        def __init__(self, seed, **kw):
+            self.seed = seed
+            calls.append((seed, kw))
+
+        def solve(self, prob):
+            return FakeResult(self.seed)
+
+        def close(self):
+            pass
+
+    class P:
+        skip = 2
+    r = parity.run_replicas(FakeCtx, P(), [3, 4, 5], mode=2)
+    assert [c[0] for c in calls] == [3, 4, 5] and all(c[1] == {"mode": 2} for c in calls)
+    assert np.allclose(r["k_samples"], [1.0003, 1.0004, 1.0005]) and r["flux_samples"].shape == (3, 4)
