@@ -371,10 +371,10 @@ def measure_batched(seed: int, device: int, steps: int, warmup: int = 3):
     return out
 
 
-def measure_serving(seed: int, device: int, seconds: float, rate: float):
+def measure_serving(seed: int, device: int, seconds: float, rate: float, drain_seconds: float = 60.0):
     from nraps_gb300 import api, serving
     ctx = api.Context(seed=seed, device=device, **ARMS["event"])
-    r = serving.run_poisson(ctx, rate=rate, seconds=seconds, seed=seed)
+    r = serving.run_poisson(ctx, rate=rate, seconds=seconds, seed=seed, drain_seconds=drain_seconds)
     ctx.close()
     return r
 
@@ -497,12 +497,18 @@ def main():
     ap.add_argument("--batched-steps", type=int, default=10, help="timed generations of the 256-instance batch (0 = skip)")
     ap.add_argument("--serve-seconds", type=float, default=20.0, help="Poisson arrival window of the serving run (0 = skip)")
     ap.add_argument("--serve-rate", type=float, default=200.0)
+    ap.add_argument("--serve-sweep", default="400,800",
+                    help="further Poisson rates (req/s) served for --serve-sweep-seconds each, up to and past "
+                         "the saturation knee ('' = none)")
+    ap.add_argument("--serve-sweep-seconds", type=float, default=10.0)
     ap.add_argument("--shape", type=lambda v: tuple(int(x) for x in v.split(",")), default=None,
                     help="block,events_per_pass,passes[,tail_lanes]: fixed event launch shape (profiling)")
     ap.add_argument("--sort", type=int, default=0, help="sorted transport with this many rounds (profiling)")
     ap.add_argument("--initial-source", type=int, default=0, help="1 = start from the diffusion fission source")
     ap.add_argument("--range", type=int, default=0, help="ranged launches of this many histories (profiling)")
     ap.add_argument("--scale-stress", type=int, default=1, help="1 = also run the 10M-history, 200k-cell slab")
+    ap.add_argument("--histories", type=int, default=0,
+                    help="histories per generation of the timed workload instead of its own (profiling)")
     ap.add_argument("--parity", type=int, default=1,
                     help="1 = event FP32 vs plain FP64 on the full workload (k, flux chi^2, time to 50 pcm)")
     ap.add_argument("--plain-small", type=int, default=1, help="1 = also run config 0 (CPU port vs plain FP64)")
@@ -524,6 +530,8 @@ def main():
     api.load()
     seed = replica_seed(args.seed, rank)
     prob = make_workload(args.workload, args.seed, args.warmup, args.steps)
+    if args.histories:
+        prob = prob.with_(histories=args.histories)
 
     # no fallback: if the chosen form cannot run, the bench fails
     arm = args.arm
@@ -612,6 +620,12 @@ def main():
     scale = measure_scale_stress(args.seed, local) if args.scale_stress and arm == "event" else None
     serving = (measure_serving(args.seed, local, args.serve_seconds, args.serve_rate)
                if args.serve_seconds > 0 and arm == "event" else None)
+    sweep = None
+    if args.serve_seconds > 0 and arm == "event" and args.serve_sweep:
+        # past the knee the queue grows without bound: the window's throughput
+        # is the measure, and the drain after the window is capped at 10 s
+        sweep = [measure_serving(args.seed, local, args.serve_sweep_seconds, float(r), drain_seconds=10.0)
+                 for r in args.serve_sweep.split(",") if r]
 
     if rank == 0:
         line = {
@@ -627,7 +641,7 @@ def main():
             "gpu_launches": d["launches"], "launch_shape": d["tuning"],
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "plain": plain, "clocks": clk,
             "fp32_vs_fp64": fp, "plain_small": small,
-            "batched": batched, "serving": serving, "scale_stress": scale,
+            "batched": batched, "serving": serving, "serving_sweep": sweep, "scale_stress": scale,
         }
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -391,6 +391,14 @@ void nraps_server_opts_default(nraps_server_opts* o);
 int  nraps_server_create(nraps_ctx* ctx, const nraps_server_opts* o, nraps_server** out);
 /* copies the problem; NRAPS_ERR_REJECTED if it can never fit the budget */
 int  nraps_server_submit(nraps_server* s, const nraps_problem* p, uint64_t seed, uint64_t* req_id);
+/* One step: admit waiting requests in arrival order while a slot and the
+   HBM budget allow, run every admitted request together for as many
+   generations as no request could retire within (each needs
+   max(2, min_active) active generations before its k can count as
+   converged, and stops at its Generations), at most 4, then read back every
+   request's k statistics and retire the converged (or capped) ones.
+   Admitted requests' buffers come from the context's stream-ordered memory
+   pool, so admissions and retirements do not synchronise the device. */
 int  nraps_server_step(nraps_server* s, uint32_t* n_running, uint32_t* n_finished);
 /* Ids of requests retired since the last call (oldest first), at most cap;
    *n receives how many were written. */

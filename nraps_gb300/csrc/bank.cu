@@ -237,6 +237,14 @@ __global__ void finalize_state(FinalizeArgs a) {
 
 }  // namespace
 
+void preload_bank_kernels() {
+    cudaFuncAttributes fa;
+    cudaFuncGetAttributes(&fa, scan_tile_sums);
+    cudaFuncGetAttributes(&fa, scan_top);
+    cudaFuncGetAttributes(&fa, scan_apply);
+    cudaFuncGetAttributes(&fa, scan_apply_carry);
+}
+
 int launch_exclusive_scan(const uint32_t* count, uint64_t n, uint32_t* block_sums, uint32_t* offsets,
                           unsigned long long* total, cudaStream_t s, bool pdl) {
     uint64_t nb = (n + SCAN_TILE - 1) / SCAN_TILE;

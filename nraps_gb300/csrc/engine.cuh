@@ -138,6 +138,9 @@ template <class T>
 int launch_plain(const PlainArgs<T>& a, int mode, int block, cudaStream_t s);
 int launch_bank_order(const BankArgs& a, cudaStream_t s);
 /* offsets[i] = sum(count[0..i)), offsets[n] = total (offsets has n+1 slots) */
+/* Load the scan kernels now (lazy module loading would otherwise load them
+   inside the first generation that launches them). */
+void preload_bank_kernels();
 int launch_exclusive_scan(const uint32_t* count, uint64_t n, uint32_t* block_sums, uint32_t* offsets,
                           unsigned long long* total, cudaStream_t s, bool pdl = false);
 /* the scan works on tiles of 2^NR_SCAN_TILE_LOG2 counts; up to

@@ -1975,6 +1975,45 @@ int launch_passes(const EvArgs& a, const EvParams& prm, int grid, size_t smem, u
 }
 }  // namespace
 
+namespace {
+/* Every kernel a generation of this engine can launch, loaded up front: with
+   lazy module loading a kernel is loaded inside the first launch that uses
+   it, and the autotuner times each candidate shape by one generation. */
+template <bool EXACT, bool BANK>
+void preload_kernels() {
+    static bool done[64] = {};           /* per device (modules load per context) */
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64 || done[dev]) return;
+    done[dev] = true;
+    cudaFuncAttributes fa;
+    auto L = [&](const void* f) { cudaFuncGetAttributes(&fa, f); };
+    L((const void*)pass_kernel<true, 1, EXACT, BANK, false, true>());
+    L((const void*)pass_kernel<true, 1, EXACT, BANK, false, false>());
+    L((const void*)pass_kernel<false, 1, EXACT, BANK, false, false>());
+    L((const void*)pass_kernel<true, 0, EXACT, BANK, false, true>());
+    L((const void*)pass_kernel<true, 0, EXACT, BANK, false, false>());
+    L((const void*)pass_kernel<false, 0, EXACT, BANK, false, false>());
+    L((const void*)pass_kernel<true, 2, EXACT, BANK, false, true>());
+    L((const void*)pass_kernel<true, 3, EXACT, BANK, false, true>());
+    L((const void*)ev_pass_wide<2, EXACT, BANK>);
+    L((const void*)ev_pass_wide<3, EXACT, BANK>);
+    L((const void*)ev_sort_flight<true, EXACT, BANK>);
+    L((const void*)ev_sort_flight<false, EXACT, BANK>);
+    L((const void*)ev_sort_collide<BANK>);
+    L((const void*)ev_finalize);
+    if (BANK) {
+        L((const void*)ev_scatter_hist);
+        L((const void*)ev_scatter<SCAT_ONE>);
+        L((const void*)ev_scatter<SCAT_TAB>);
+        L((const void*)ev_scatter<SCAT_DIRECT>);
+        L((const void*)ev_rb_scan);
+        L((const void*)ev_rb_scatter);
+        preload_bank_kernels();
+    }
+}
+}  // namespace
+
 int EventEngine::commit(cudaStream_t s, std::string& err) {
     Impl& m = *impl_;
     if (m.inst.empty()) { err = "no instances"; return NRAPS_ERR_INVALID; }
@@ -2083,6 +2122,8 @@ int EventEngine::commit(cudaStream_t s, std::string& err) {
         }
     }
     a.nlog2n = m.nlog2n.p;
+    if (bank) { if (m.exact) preload_kernels<true, true>(); else preload_kernels<false, true>(); }
+    else { if (m.exact) preload_kernels<true, false>(); else preload_kernels<false, false>(); }
     m.committed = true;
     return size_grid();
 }

@@ -7,8 +7,9 @@ per generation are log-uniform in [10k, 500k].  Every request carries the
 accuracy target: it is done when the standard error of its k over its active
 generations is at most sigma_k_target (after at least min_active active
 generations).  The driver submits each request at its arrival time, steps the
-server (one generation of every admitted request per step), and records the
-time from arrival to completion.
+server (one to four generations of every admitted request per step: as many
+as no request could retire within), and records the time from arrival to
+completion.
 """
 from __future__ import annotations
 
@@ -52,8 +53,11 @@ def run_poisson(ctx: api.Context, rate: float = 200.0, seconds: float = 20.0, se
     nxt = 0
     steps = 0
     busy0 = srv.stats()["busy_ms"]
+    window_hist = None           # histories simulated by the end of the arrival window
     while True:
         now = srv.clock - t0
+        if window_hist is None and now >= seconds:
+            window_hist = srv.stats()["histories"]
         while nxt < n_req and arrivals[nxt] <= now:
             p = pool[geo[nxt]].with_(histories=int(sizes[nxt]))
             try:
@@ -95,6 +99,7 @@ def run_poisson(ctx: api.Context, rate: float = 200.0, seconds: float = 20.0, se
         "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
         "mean_generations": float(np.mean(gens)) if gens else 0.0,
         "histories_per_s": st["histories"] / elapsed if elapsed > 0 else 0.0,
+        "window_histories_per_s": (window_hist if window_hist is not None else st["histories"]) / seconds,
         "completed_histories": int(hist_done), "elapsed_s": elapsed, "steps": steps,
         "gpu_busy_fraction": (st["busy_ms"] - busy0) / 1000.0 / elapsed if elapsed > 0 else 0.0,
         "sigma_k_target": sigma_k_target, "min_active": min_active, "inactive": inactive,
