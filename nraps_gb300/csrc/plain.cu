@@ -198,6 +198,7 @@ __device__ void physics_history(const PlainArgs<T>& a, uint64_t h, uint64_t seed
        dividing per crossing, and the history's k score is one fused
        multiply-add per track piece, fixed to 2^-32 once per history */
     T inv_mu = mu != T(0) ? T(1) / mu : inf;
+    bool fwd = mu >= T(0), flat = mu == T(0);     /* set with mu */
     double ks = 0.0;
     for (;;) {
         rec.segments++;
@@ -208,9 +209,8 @@ __device__ void physics_history(const PlainArgs<T>& a, uint64_t h, uint64_t seed
         bool stop = false, same = true;
         while (same) {
             if (++events > a.max_events) { fate = NRAPS_FATE_CAPPED; stop = true; break; }
-            const bool fwd = mu >= T(0);
             T face = fwd ? __ldg(&a.right[cell]) : __ldg(&a.left[cell]);
-            T lf = (mu != T(0)) ? (face - x) * inv_mu : inf;
+            T lf = flat ? inf : (face - x) * inv_mu;
             if (lf < l) {
                 atomicAdd(&a.tally[(uint64_t)g * a.nc + cell], (double)lf);
                 ks = __fma_rn(nsf, (double)lf, ks);
@@ -218,7 +218,7 @@ __device__ void physics_history(const PlainArgs<T>& a, uint64_t h, uint64_t seed
                 l = l - lf; x = face;
                 if (fwd ? (cell == last) : (cell == 0)) {
                     T bound = fwd ? a.boundr : a.boundl;
-                    if (bound > T(0)) { mu = -mu; inv_mu = -inv_mu; rec.reflections++; }
+                    if (bound > T(0)) { mu = -mu; inv_mu = -inv_mu; fwd = !fwd; rec.reflections++; }
                     else { fate = NRAPS_FATE_LEAKED; stop = true; break; }
                 } else {
                     cell = fwd ? cell + 1 : cell - 1;
@@ -249,6 +249,8 @@ __device__ void physics_history(const PlainArgs<T>& a, uint64_t h, uint64_t seed
                 g = ng;
                 mu = T(2) * u01<T>(rng.next()) - T(1);
                 inv_mu = mu != T(0) ? T(1) / mu : inf;
+                fwd = mu >= T(0);
+                flat = mu == T(0);
                 xs = m + (uint64_t)M * g;
                 nsf = (double)__ldg(&a.nsf[xs]);
                 l = -lg(upos<T>(rng.next())) * __ldg(&a.inv_sigtr[xs]);
