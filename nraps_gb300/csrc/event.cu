@@ -2050,7 +2050,9 @@ uint64_t EventEngine::shared_bytes() const {
 namespace {
 template <bool SOURCE, int ONE, bool EXACT, bool BANK, bool REC, bool OP>
 void set_smem_attr(size_t smem) {
-    static size_t granted = 48 * 1024;          /* the default dynamic limit         */
+    /* the default limit of dynamic shared memory is 48 KB less the kernel's
+       static shared memory: raise it for any dynamic size asked for */
+    static size_t granted = 0;
     if (smem > granted) {
         cudaFuncSetAttribute(pass_kernel<SOURCE, ONE, EXACT, BANK, REC, OP>(),
                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -2293,7 +2295,7 @@ int EventEngine::size_grid() {
                                       : (const void*)pass_kernel<true, 1, false, true, false, true>())
                            : (const void*)pass_kernel<true, 0, false, true, false, true>();
     const size_t dyn = stage_bytes(params.block) + (m.one ? m.smem_bytes : 0);
-    if (dyn > 48 * 1024) cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+    cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, (int)params.block, dyn) != cudaSuccess ||
         per_sm < 1)
         per_sm = 1;
@@ -2426,7 +2428,7 @@ int EventEngine::enqueue_generation(cudaStream_t s, bool with_finalize, cudaEven
     if (bank && ar.rb) {
         launch_k(m.pdl, ev_rb_scan, dim3(a.n_inst), dim3(RB_THREADS), 0, s, ar);
         const size_t hb = ((size_t)ar.range_len + m.rb_hist_cells) * 4;
-        if (hb > 48 * 1024) cudaFuncSetAttribute(ev_rb_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hb);
+        if (hb > 40 * 1024) cudaFuncSetAttribute(ev_rb_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hb);
         launch_k(m.pdl, ev_rb_scatter, dim3(m.ranged_blocks), dim3(RB_THREADS), hb, s, ar);
         n += 2;
     } else if (bank) {
@@ -2435,7 +2437,7 @@ int EventEngine::enqueue_generation(cudaStream_t s, bool with_finalize, cudaEven
         n += q;
         if (a.hist_smem) {
             const size_t hb = (size_t)m.inst[0]->d.nc * 4;
-            if (hb > 48 * 1024)
+            if (hb > 40 * 1024)
                 cudaFuncSetAttribute(ev_scatter_hist, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hb);
             launch_k(m.pdl, ev_scatter_hist, dim3(NSLAB * SCATTER_ONE_SPLIT), dim3(SCATTER_ONE_THREADS), hb, s, a);
         } else if (m.one || rec) {
