@@ -192,14 +192,9 @@ struct TView {
     const float4* rdat;
     const uint2* bins;
     const uint8_t* rmat;
-    const uint8_t* cmat;          /* per cell: births look up their material */
-    const float* chi_birth;       /* chi CDFs for births                      */
-    uint32_t G, R, nbins, nc_cells;
+    uint32_t G, R, nbins;
     float L, inv_binw, boundl, boundr;
 };
-
-/* cells whose materials a staged table set carries in shared memory */
-constexpr uint32_t CMAT_SMEM_MAX = 16384;
 
 __device__ __forceinline__ float u24(uint32_t u) { return __fmul_rn(__uint2float_rn(u >> 8), 0x1p-24f); }
 __device__ __forceinline__ float u24pos(uint32_t u) { return __fmul_rn(__uint2float_rn((u >> 8) + 1u), 0x1p-24f); }
@@ -302,7 +297,6 @@ __device__ __forceinline__ TView global_view(const EvInst& I) {
     TView t;
     t.xs = reinterpret_cast<const float4*>(I.xs); t.inv_st64 = I.inv_st64; t.kq = I.kq; t.ocdf = I.ocdf;
     t.chi = I.chicdf; t.maj = I.maj; t.rdat = I.rdat; t.bins = I.bins; t.rmat = I.rmat;
-    t.cmat = I.cmat; t.chi_birth = I.chicdf; t.nc_cells = I.nc;
     t.G = I.G; t.R = I.R; t.nbins = I.nbins; t.L = I.L; t.inv_binw = I.inv_binw;
     t.boundl = I.boundl; t.boundr = I.boundr;
     return t;
@@ -310,11 +304,10 @@ __device__ __forceinline__ TView global_view(const EvInst& I) {
 
 /* shared-memory footprint of one instance's tables: 8-byte and 16-byte
    arrays first, then floats, then bytes */
-__host__ __device__ __forceinline__ size_t smem_bytes_for(uint32_t M, uint32_t G, uint32_t R, uint32_t nbins,
-                                                         uint32_t nc) {
+__host__ __device__ __forceinline__ size_t smem_bytes_for(uint32_t M, uint32_t G, uint32_t R, uint32_t nbins) {
     const size_t MG = (size_t)M * G;
     size_t b = MG * 16 + MG * 16 + ((size_t)R + 1) * 16 + (size_t)nbins * 8;
-    b += (MG * G + MG + 2 * (size_t)G) * 4 + R + (nc <= CMAT_SMEM_MAX ? nc : 0);
+    b += (MG * G + MG + 2 * (size_t)G) * 4 + R;
     return (b + 15) / 16 * 16;
 }
 
@@ -331,8 +324,6 @@ __device__ __forceinline__ void stage_tables(const EvInst& I, unsigned char* tab
     float* s_chi = s_ocdf + MG * G;
     float* s_maj = s_chi + MG;
     uint8_t* s_rmat = reinterpret_cast<uint8_t*>(s_maj + 2 * G);
-    uint8_t* s_cmat = s_rmat + R;
-    const bool cm = I.nc <= CMAT_SMEM_MAX;
     const float4* g_xs = reinterpret_cast<const float4*>(I.xs);
     for (uint32_t i = threadIdx.x; i < MG; i += blockDim.x) {
         s_inv64[i] = I.inv_st64[i]; s_kq[i] = I.kq[i]; s_xs[i] = g_xs[i];
@@ -343,13 +334,8 @@ __device__ __forceinline__ void stage_tables(const EvInst& I, unsigned char* tab
     for (uint32_t i = threadIdx.x; i < MG; i += blockDim.x) s_chi[i] = I.chicdf[i];
     for (uint32_t i = threadIdx.x; i < 2 * G; i += blockDim.x) s_maj[i] = I.maj[i];
     for (uint32_t i = threadIdx.x; i < R; i += blockDim.x) s_rmat[i] = I.rmat[i];
-    if (cm)
-        for (uint32_t i = threadIdx.x; i < I.nc; i += blockDim.x) s_cmat[i] = I.cmat[i];
     t.xs = s_xs; t.inv_st64 = s_inv64; t.kq = s_kq; t.ocdf = s_ocdf; t.chi = s_chi; t.maj = s_maj;
     t.rdat = s_rdat; t.bins = s_bins; t.rmat = s_rmat;
-    t.cmat = cm ? s_cmat : I.cmat;
-    t.chi_birth = s_chi;
-    t.nc_cells = I.nc;
     t.G = G; t.R = R; t.nbins = NB; t.L = I.L; t.inv_binw = I.inv_binw;
     t.boundl = I.boundl; t.boundr = I.boundr;
 }
@@ -368,18 +354,7 @@ struct Stage {
     /* prefetched input records of the warp's current chunk */
     uint4 pf_a[CHUNK];
     unsigned long long pf_rng[CHUNK];
-    /* bank sites of the warp's next chunk, copied asynchronously */
-    uint4 raw[CHUNK];
 };
-
-/* 16-byte global -> shared copy that does not wait (cp.async, bypassing L1);
-   cp_async_wait() waits for every copy this thread has issued */
-__device__ __forceinline__ void cp_async16(void* smem_dst, const void* gsrc) {
-    const unsigned d = (unsigned)__cvta_generic_to_shared(smem_dst);
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" :: "r"(d), "l"(gsrc) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
 static_assert(sizeof(Stage) % 16 == 0, "Stage keeps the tables after it 16-byte aligned");
 __host__ __device__ __forceinline__ size_t stage_bytes(uint32_t block) { return (size_t)(block / 32) * sizeof(Stage); }
@@ -410,21 +385,6 @@ __device__ __forceinline__ bool flush_sites(const EvArgs& a, S& sg, uint32_t n, 
     base = __shfl_sync(0xffffffffu, base, 0);
     if (base + n > a.slab_cap) return false;
     for (uint32_t i = lane; i < n; i += 32) a.sites[(uint64_t)slab * a.slab_cap + base + i] = sg.site[i];
-    return true;
-}
-
-/* Slab slots reserved one flush ahead: when a warp has staged SITE_RESERVE_AT
-   sites, lane 0 reserves 32 slots of its slab (the atomic's result is read
-   only at the flush), so the round trip overlaps the warp's flights.  A
-   reservation that is not filled when the warp ends is padded with records
-   whose parent is 0xFFFFFFFF, which the bank scatter skips. */
-constexpr uint32_t SITE_RESERVE_AT = 8;
-template <class S>
-__device__ __forceinline__ bool flush_sites_reserved(const EvArgs& a, S& sg, uint32_t n, uint32_t slab, uint32_t lane,
-                                                     unsigned long long res) {
-    const unsigned long long base = __shfl_sync(0xffffffffu, res, 0);
-    if (base + 32 > a.slab_cap) return false;
-    a.sites[(uint64_t)slab * a.slab_cap + base + lane] = lane < n ? sg.site[lane] : make_uint4(0u, 0u, 0xFFFFFFFFu, 0u);
     return true;
 }
 
@@ -579,8 +539,6 @@ __device__ __forceinline__ void ev_pass_body(const EvArgs& a, int pass, uint32_t
     uint64_t pf_base = 0;                   /* first index of the prefetch    */
     bool exhausted = false;
     uint32_t staged = 0, staged_sites = 0;  /* warp-uniform                   */
-    unsigned long long sres = 0;             /* lane 0: reserved slab slots      */
-    bool res_on = false;                     /* warp-uniform: a reservation is out */
     bool slab_full = false;
     Acc acc = {0, 0, 0, 0, 0, 0};
     bool have = false;
@@ -595,74 +553,12 @@ __device__ __forceinline__ void ev_pass_body(const EvArgs& a, int pass, uint32_t
     unsigned long long kq_part = 0;          /* batched: lane's k score for kq_inst */
     uint32_t kq_inst = 0;
     uint32_t draws = 0;
-    /* PF: single-instance source launches from a non-empty bank pipeline
-       their input.  When a warp starts a chunk it claims the next one; once
-       half the chunk is handed out (the claim is back by then) it issues
-       asynchronous copies of the next chunk's bank sites into shared memory;
-       when the chunk runs out, the next one's births are computed from
-       shared memory.  The claim's round trip and the sites' loads overlap
-       the flights instead of stalling the warp. */
-    constexpr bool PF_T = SOURCE && BANK && (ONE == 1 || ONE == 2) && !REC;
-    const bool PF = PF_T && s_src.nbk > 0;
-    unsigned long long ahead = 0;            /* lane 0: base of the next chunk   */
-    uint32_t ahead_state = 0;                /* 0 none, 1 claimed, 2 copies issued */
     for (;;) {
-        if (PF_T && PF && ahead_state == 1 && pool_next - pf_base >= CHUNK / 2) {
-            const unsigned long long nb = __shfl_sync(FULL, ahead, 0);
-            if (nb < n_in) {
-                const uint64_t ne = nb + CHUNK < n_in ? nb + CHUNK : n_in;
-                const unsigned long long hb = s_hot[0].hist_begin;
-                __syncwarp();
-                for (uint32_t k = lane; k < (uint32_t)(ne - nb); k += 32)
-                    cp_async16(&sg.raw[k], reinterpret_cast<const uint4*>(s_src.bank) +
-                                               bank_site(nb + k - hb, s_src.nbk, s_src.ndiv));
-                cp_async_commit();
-            }
-            ahead_state = 2;
-        }
         /* ---- hand input particles to idle lanes ----------------------------
            A warp claims CHUNK input particles with one atomic and prefetches
            their records (birth site + instance, or queue entry) into shared
            memory in one coalesced step; idle lanes then take them in order. */
         unsigned need = __ballot_sync(FULL, !have);
-        if (PF_T && PF && need && !exhausted && pool_next == pool_end) {
-            unsigned long long base = ahead;
-            if (ahead_state == 0 && lane == 0) base = atomicAdd(claim, (unsigned long long)CHUNK);
-            base = __shfl_sync(FULL, base, 0);
-            if (base >= n_in) {
-                exhausted = true;
-            } else {
-                pool_next = base;
-                pool_end = base + CHUNK < n_in ? base + CHUNK : n_in;
-                const unsigned long long hb = s_hot[0].hist_begin, gseed = s_hot[0].gseed;
-                __syncwarp();              /* every lane is done with the last chunk */
-                if (ahead_state != 2) {
-                    for (uint32_t k = lane; k < (uint32_t)(pool_end - pool_next); k += 32)
-                        cp_async16(&sg.raw[k], reinterpret_cast<const uint4*>(s_src.bank) +
-                                                   bank_site(pool_next + k - hb, s_src.nbk, s_src.ndiv));
-                    cp_async_commit();
-                }
-                /* each lane reads only the sites it copied itself */
-                cp_async_wait();
-                for (uint32_t k = lane; k < (uint32_t)(pool_end - pool_next); k += 32) {
-                    const uint64_t idx = pool_next + k;
-                    const uint4 sv = sg.raw[k];
-                    nr_pcg32 rng = nr_pcg32_seeded(gseed, (uint32_t)(idx - hb));
-                    /* the birth of a banked particle, as below */
-                    const float bmu = __fsub_rn(__fmul_rn(2.0f, u24(nr_pcg32_next(&rng))), 1.0f);
-                    const uint32_t c = sv.y < t.nc_cells ? sv.y : t.nc_cells - 1;
-                    const uint32_t bg = count_below(t.chi_birth + (uint32_t)t.cmat[c] * t.G, t.G,
-                                                    u24(nr_pcg32_next(&rng)));
-                    sg.pf_a[k] = make_uint4(sv.x, __float_as_uint(bmu), (uint32_t)idx, bg | (inst0 << 4));
-                    sg.pf_rng[k] = rng.state;
-                }
-                pf_base = pool_next;
-                __syncwarp();
-                /* claim the next chunk now: it is needed half a chunk later */
-                if (lane == 0) ahead = atomicAdd(claim, (unsigned long long)CHUNK);
-                ahead_state = 1;
-            }
-        }
         if (need && !exhausted) {
             if (pool_next == pool_end) {
                 unsigned long long base = 0;
@@ -731,8 +627,7 @@ __device__ __forceinline__ void ev_pass_body(const EvArgs& a, int pass, uint32_t
                                    of the material it was born in */
                                 bmu = __fsub_rn(__fmul_rn(2.0f, u24(nr_pcg32_next(&rng))), 1.0f);
                                 const uint32_t c = bcell < I.nc ? bcell : I.nc - 1;
-                                bg = ONE ? count_below(t.chi_birth + (uint32_t)t.cmat[c] * I.G, I.G, u24(nr_pcg32_next(&rng)))
-                                         : count_below(I.chicdf + (uint32_t)I.cmat[c] * I.G, I.G, u24(nr_pcg32_next(&rng)));
+                                bg = count_below(I.chicdf + (uint32_t)I.cmat[c] * I.G, I.G, u24(nr_pcg32_next(&rng)));
                             } else {
                                 /* fresh uniform fuel source (spawn_neutron) */
                                 const uint32_t cell = I.fuel[((uint64_t)nr_pcg32_next(&rng) * I.nfuel) >> 32];
@@ -901,22 +796,13 @@ __device__ __forceinline__ void ev_pass_body(const EvArgs& a, int pass, uint32_t
                     pending--;
                 }
                 staged_sites += __popc(sm);
-                if (!rbk && !res_on && staged_sites >= SITE_RESERVE_AT) {
-                    if (lane == 0) sres = atomicAdd(&a.slab_count[slab], 32ULL);
-                    res_on = true;
-                }
                 __syncwarp();
                 if (staged_sites >= 32) {
                     const bool fl = rbk ? flush_range_sites(a, sg, 32, lane, &s_rfill, s_rchunk, &Ip->st->error)
-                                        : flush_sites_reserved(a, sg, 32, slab, lane, sres);
+                                        : flush_sites(a, sg, 32, slab, lane);
                     if (!fl) slab_full = true;
                     move_down(sg, 32, staged_sites - 32, lane, true);
                     staged_sites -= 32;
-                    res_on = false;
-                    if (!rbk && staged_sites >= SITE_RESERVE_AT) {
-                        if (lane == 0) sres = atomicAdd(&a.slab_count[slab], 32ULL);
-                        res_on = true;
-                    }
                 }
             }
         }
@@ -972,10 +858,7 @@ __device__ __forceinline__ void ev_pass_body(const EvArgs& a, int pass, uint32_t
     __syncwarp();
     if (!ONE && kq_part) atomicAdd(&a.inst[kq_inst].st->kq, kq_part);
     if (staged) flush_particles(a, sg, staged, pass, qout, lane);
-    if (BANK && !rbk && res_on) {
-        /* the staged sites (fewer than 32) and padding into the reservation */
-        if (!flush_sites_reserved(a, sg, staged_sites, slab, lane, sres)) slab_full = true;
-    } else if (BANK && staged_sites) {
+    if (BANK && staged_sites) {
         const bool fl = rbk ? flush_range_sites(a, sg, staged_sites, lane, &s_rfill, s_rchunk, &Ip->st->error)
                             : flush_sites(a, sg, staged_sites, slab, lane);
         if (!fl) slab_full = true;
@@ -2214,7 +2097,7 @@ int EventEngine::commit(cudaStream_t s, std::string& err) {
     m.smem_bytes = 0;
     if (n == 1) {
         const EvInst& I = m.inst[0]->d;
-        size_t sb = smem_bytes_for(I.M, I.G, I.R, I.nbins, I.nc);
+        size_t sb = smem_bytes_for(I.M, I.G, I.R, I.nbins);
         if (sb <= 120 * 1024) { m.one = true; m.smem_bytes = sb; }
     }
     a.hist_smem = (m.one && bank && m.inst[0]->d.nc <= HIST_SMEM_MAX_CELLS) ? 1 : 0;
@@ -2225,7 +2108,7 @@ int EventEngine::commit(cudaStream_t s, std::string& err) {
         size_t tmax = 0;
         for (uint32_t i = 0; i < n; ++i) {
             const EvInst& I = m.inst[i]->d;
-            tmax = std::max(tmax, smem_bytes_for(I.M, I.G, I.R, I.nbins, I.nc));
+            tmax = std::max(tmax, smem_bytes_for(I.M, I.G, I.R, I.nbins));
         }
         m.ranged_fit = tmax <= RANGED_SMEM_MAX;
         m.ranged_smem = (tmax + 15) / 16 * 16;
