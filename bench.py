@@ -495,7 +495,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
     ap.add_argument("--batched-steps", type=int, default=10, help="timed generations of the 256-instance batch (0 = skip)")
-    ap.add_argument("--serve-seconds", type=float, default=20.0, help="Poisson arrival window of the serving run (0 = skip)")
+    ap.add_argument("--serve-seconds", type=float, default=60.0, help="Poisson arrival window of the serving run (config 3: 60 s; 0 = skip)")
     ap.add_argument("--serve-rate", type=float, default=200.0)
     ap.add_argument("--serve-sweep", default="400,800",
                     help="further Poisson rates (req/s) served for --serve-sweep-seconds each, up to and past "
