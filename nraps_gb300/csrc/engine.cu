@@ -215,6 +215,9 @@ using nrint::validate_problem;
 }  // namespace
 
 struct nraps_session {
+    /* small buffers of the session and its engine, each on its own 64 KB
+       (declared first: destroyed after every buffer it handed out) */
+    DeviceArena arena;
     nraps_ctx* ctx = nullptr;
     nraps_opts o{};
     nraps_variables v{};
@@ -293,35 +296,35 @@ int create_session(nraps_ctx* ctx, const nraps_problem* p, bool with_records, nr
                                                  : build_tables<double>(*p, blob, s->L, err);
     if (bt) return set_err(ctx, NRAPS_ERR_INVALID, err);
     cudaStream_t sm = ctx->stream;
-    CK(s->tables.alloc(blob.size()));
+    CK(s->tables.alloc_in(s->arena, blob.size()));
     CK(cudaMemcpyAsync(s->tables.p, blob.data(), blob.size(), cudaMemcpyHostToDevice, sm));
     uint64_t nb = s->G * s->nc;
-    CK(s->tally.alloc(nb * 8));
-    CK(s->flux_acc.alloc(nb * 8)); CK(s->flux_sum.alloc(nb * 8)); CK(s->flux_sq.alloc(nb * 8));
-    CK(s->fs_acc.alloc(s->nc * 8));
-    CK(s->k64.alloc(s->gens * 8)); CK(s->entropy.alloc(s->gens * 8));
-    CK(s->state.alloc(sizeof(GenState)));
+    CK(s->tally.alloc_in(s->arena, nb * 8));
+    CK(s->flux_acc.alloc_in(s->arena, nb * 8)); CK(s->flux_sum.alloc_in(s->arena, nb * 8)); CK(s->flux_sq.alloc_in(s->arena, nb * 8));
+    CK(s->fs_acc.alloc_in(s->arena, s->nc * 8));
+    CK(s->k64.alloc_in(s->arena, s->gens * 8)); CK(s->entropy.alloc_in(s->arena, s->gens * 8));
+    CK(s->state.alloc_in(s->arena, sizeof(GenState)));
     uint32_t nfb = finalize_blocks_for(s->nc);
-    CK(s->partials.alloc(2 * (size_t)nfb * 8));
+    CK(s->partials.alloc_in(s->arena, 2 * (size_t)nfb * 8));
     bool bank = s->o.mode == NRAPS_MODE_BANK;
     bool woodcock = s->o.tracking == NRAPS_TRACK_WOODCOCK;
     double bf = s->o.bank_factor > 0 ? s->o.bank_factor : 3.0;
     s->cap = bank ? (uint64_t)(bf * (double)s->N) + 1024 : 0;
     if (bank) {
         if (!woodcock) {   /* the event engine keeps its own site slabs */
-            CK(s->sx.alloc(s->cap * 4)); CK(s->scell.alloc(s->cap * 4)); CK(s->sgroup.alloc(s->cap * 4));
-            CK(s->sparent.alloc(s->cap * 4)); CK(s->sseq.alloc(s->cap * 4));
-            CK(s->scount.alloc(s->n_hist * 4)); CK(s->offsets.alloc((s->n_hist + 1) * 4));
-            CK(s->block_sums.alloc(((s->n_hist + 4095) / 4096 + 1) * 4));
+            CK(s->sx.alloc_in(s->arena, s->cap * 4)); CK(s->scell.alloc_in(s->arena, s->cap * 4)); CK(s->sgroup.alloc_in(s->arena, s->cap * 4));
+            CK(s->sparent.alloc_in(s->arena, s->cap * 4)); CK(s->sseq.alloc_in(s->arena, s->cap * 4));
+            CK(s->scount.alloc_in(s->arena, s->n_hist * 4)); CK(s->offsets.alloc_in(s->arena, (s->n_hist + 1) * 4));
+            CK(s->block_sums.alloc_in(s->arena, ((s->n_hist + 4095) / 4096 + 1) * 4));
             CK(cudaMemsetAsync(s->scount.p, 0, s->n_hist * 4, sm));
         }
-        CK(s->bank0.alloc(s->cap * sizeof(nraps_site))); CK(s->bank1.alloc(s->cap * sizeof(nraps_site)));
+        CK(s->bank0.alloc_in(s->arena, s->cap * sizeof(nraps_site))); CK(s->bank1.alloc_in(s->arena, s->cap * sizeof(nraps_site)));
         uint64_t hist_words = woodcock ? ev_hist_words(s->nc) : s->nc;
-        CK(s->hist.alloc(hist_words * 4));
+        CK(s->hist.alloc_in(s->arena, hist_words * 4));
         CK(cudaMemsetAsync(s->hist.p, 0, hist_words * 4, sm));
     }
     if (with_records) {
-        CK(s->records.alloc(s->n_hist * sizeof(nraps_history_record)));
+        CK(s->records.alloc_in(s->arena, s->n_hist * sizeof(nraps_history_record)));
         CK(cudaMemsetAsync(s->records.p, 0, s->n_hist * sizeof(nraps_history_record), sm));
     }
     CK(cudaMemsetAsync(s->tally.p, 0, nb * 8, sm));
@@ -385,6 +388,7 @@ int create_session(nraps_ctx* ctx, const nraps_problem* p, bool with_records, nr
     f.bank_cap = s->cap;
     if (woodcock) {
         s->ev.reset(new EventEngine());
+        s->ev->set_arena(&s->arena);
         std::string e2;
         int est = s->ev->configure(s->o, e2);
         if (est) return set_err(ctx, est, e2);

@@ -14,6 +14,7 @@
 
 #include "../../include/nraps_gpu.h"
 #include "engine.cuh"
+#include "arena.hpp"
 #include "event.cuh"
 #include "host_common.hpp"
 
@@ -51,14 +52,24 @@ struct DevMem {
     size_t n = 0;
     cudaStream_t fs = nullptr;          /* stream-ordered: the stream it is freed on */
     bool pooled = false;
+    bool in_arena = false;              /* owned by a DeviceArena: never freed here */
     DevMem() = default;
     DevMem(const DevMem&) = delete;
     DevMem& operator=(const DevMem&) = delete;
     ~DevMem() { release(); }
     void release() {
-        if (p) { if (pooled) cudaFreeAsync(p, fs); else cudaFree(p); }
+        if (p && !in_arena) { if (pooled) cudaFreeAsync(p, fs); else cudaFree(p); }
         p = nullptr;
         pooled = false;
+        in_arena = false;
+    }
+    /* a small buffer from the arena, a large one from cudaMalloc */
+    cudaError_t alloc_in(DeviceArena& a, size_t bytes) {
+        if (bytes == 0 || bytes > DeviceArena::ITEM_MAX) return alloc(bytes);
+        release();
+        n = bytes;
+        in_arena = true;
+        return a.take(bytes, &p);
     }
     cudaError_t alloc(size_t bytes, cudaMemPool_t pool = nullptr, cudaStream_t s = nullptr) {
         release();

@@ -1722,19 +1722,26 @@ template <class T> struct DBuf {
     size_t n = 0;
     cudaStream_t fs = nullptr;       /* pooled: freed in this stream's order */
     bool pooled = false;
+    DeviceArena* arena = nullptr;    /* small buffers from here (never freed one by one) */
+    bool in_arena = false;
     DBuf() = default;
     DBuf(const DBuf&) = delete;
     DBuf& operator=(const DBuf&) = delete;
     ~DBuf() { release(); }
     void release() {
-        if (p) { if (pooled) cudaFreeAsync(p, fs); else cudaFree(p); }
+        if (p && !in_arena) { if (pooled) cudaFreeAsync(p, fs); else cudaFree(p); }
         p = nullptr;
         pooled = false;
+        in_arena = false;
     }
     cudaError_t alloc(size_t count, cudaMemPool_t pool = nullptr, cudaStream_t s = nullptr) {
         release();
         n = count;
         if (!count) return cudaSuccess;
+        if (arena && !pool && count * sizeof(T) <= DeviceArena::ITEM_MAX) {
+            in_arena = true;
+            return arena->take(count * sizeof(T), reinterpret_cast<void**>(&p));
+        }
         if (pool) {
             pooled = true;
             fs = s;
@@ -1800,6 +1807,7 @@ struct EventEngine::Impl {
     /* per-instance tables from a stream-ordered pool (set_pool), or cudaMalloc */
     cudaMemPool_t pool = nullptr;
     cudaStream_t pool_stream = nullptr;
+    DeviceArena* arena = nullptr;       /* small buffers at 64 KB strides (sessions) */
     ~Impl() { for (Inst* i : inst) delete i; }
 };
 
@@ -1847,6 +1855,7 @@ uint64_t EventEngine::table_bytes(const nraps_problem& p) {
 int EventEngine::add_instance(const nraps_problem& p, const EvBuffers& b, std::string& err) {
     if (impl_->inst.size() >= 4095) { err = "at most 4095 instances per batch"; return -1; }
     Impl::Inst* in = new Impl::Inst();
+    in->blob.arena = impl_->arena;
     if (build_event_tables(p, in->h, err)) { delete in; return -1; }
     const EvHostTables& h = in->h;
     size_t off = 0;
@@ -1918,6 +1927,19 @@ void EventEngine::clear_instances() {
 }
 
 uint32_t EventEngine::n_instances() const { return (uint32_t)impl_->inst.size(); }
+void EventEngine::set_arena(DeviceArena* a) {
+    Impl& m = *impl_;
+    m.arena = a;
+    for (DBuf<float>* b : {&m.qx[0], &m.qx[1], &m.qmu[0], &m.qmu[1], &m.cx, &m.cmu}) b->arena = a;
+    for (DBuf<unsigned long long>* b : {&m.qrng[0], &m.qrng[1], &m.qcount, &m.slab_count, &m.crng, &m.rb_base,
+                                        &m.rb_total})
+        b->arena = a;
+    for (DBuf<uint32_t>* b : {&m.qid[0], &m.qid[1], &m.qpk[0], &m.qpk[1], &m.count, &m.offsets, &m.block_sums,
+                              &m.d_range_begin, &m.rb_chunk, &m.rb_fill, &m.cid, &m.cpk, &m.creg})
+        b->arena = a;
+    m.d_inst.arena = a; m.d_inst_begin.arena = a; m.d_cell_begin.arena = a;
+    m.sites.arena = a; m.bstats.arena = a; m.nlog2n.arena = a;
+}
 void EventEngine::set_pool(cudaMemPool_t pool, cudaStream_t s) { impl_->pool = pool; impl_->pool_stream = s; }
 void EventEngine::set_records(nraps_history_record* rec) { impl_->rec = rec; impl_->committed = false; }
 const uint32_t* EventEngine::offsets() const { return impl_->offsets.p; }

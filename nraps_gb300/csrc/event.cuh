@@ -25,6 +25,7 @@
 #include <string>
 #include <vector>
 
+#include "arena.hpp"
 #include "engine.cuh"
 
 /* Per-instance device buffers owned by the caller (a session or a batch). */
@@ -81,6 +82,9 @@ public:
     /* Allocate later instances' tables stream-ordered from `pool` on `s`
        (the request server admits and retires instances every step). */
     void set_pool(cudaMemPool_t pool, cudaStream_t s);
+    /* Take every buffer of up to DeviceArena::ITEM_MAX bytes from `a` (each
+       on its own 64 KB); `a` must outlive the engine. */
+    void set_arena(DeviceArena* a);
     /* Drop one instance (later instances shift down by one). */
     void remove_instance(uint32_t idx);
     uint32_t n_instances() const;
