@@ -216,11 +216,6 @@ def measure_device(prob, arm: str, steps: int, warmup: int, seed: int, device: i
     # the flush zero_() launches are torch's, not ours; ctx.launches counts ours
     s.close()
     ctx.close()
-    # hand the flush buffer back to the driver: with 256 MB of torch's cache
-    # still reserved in front of them, the buffers of later measurements
-    # land elsewhere in memory and the transport measured 18% slower
-    del flush
-    torch.cuda.empty_cache()
     return out
 
 

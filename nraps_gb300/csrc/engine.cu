@@ -92,23 +92,24 @@ cudaMemPool_t ctx_pool(nraps_ctx* ctx) {
 }
 
 cudaError_t InstBuffers::alloc(uint64_t G_, uint64_t nc_, uint64_t gens_, uint64_t N, double bank_factor, bool bank,
-                               double k0, GenState* st_ext, cudaStream_t s, cudaMemPool_t pool) {
+                               double k0, GenState* st_ext, cudaStream_t s, cudaMemPool_t pool, DeviceArena* arena) {
     G = G_; nc = nc_; gens = gens_;
     double bf = bank_factor > 0 ? bank_factor : 3.0;
     cap = bank ? (uint64_t)(bf * (double)N) + 1024 : 0;
     uint64_t nb = G * nc;
     cudaError_t e = cudaSuccess;
     auto A = [&](cudaError_t x) { if (e == cudaSuccess) e = x; };
-    A(tally.alloc(nb * 8, pool, s)); A(flux_acc.alloc(nb * 8, pool, s)); A(flux_sum.alloc(nb * 8, pool, s));
-    A(flux_sq.alloc(nb * 8, pool, s));
-    A(fs_acc.alloc(nc * 8, pool, s)); A(k64.alloc(gens * 8, pool, s)); A(entropy.alloc(gens * 8, pool, s));
+    /* small buffers at 64 KB strides from the arena, when there is one */
+    auto take = [&](DevMem& d, size_t bytes) { A(arena ? d.alloc_in(*arena, bytes) : d.alloc(bytes, pool, s)); };
+    take(tally, nb * 8); take(flux_acc, nb * 8); take(flux_sum, nb * 8); take(flux_sq, nb * 8);
+    take(fs_acc, nc * 8); take(k64, gens * 8); take(entropy, gens * 8);
     if (bank) {
-        A(bank0.alloc(cap * sizeof(nraps_site), pool, s)); A(bank1.alloc(cap * sizeof(nraps_site), pool, s));
-        A(hist.alloc(ev_hist_words(nc) * 4, pool, s));
+        take(bank0, cap * sizeof(nraps_site)); take(bank1, cap * sizeof(nraps_site));
+        take(hist, ev_hist_words(nc) * 4);
         if (e == cudaSuccess) A(cudaMemsetAsync(hist.p, 0, ev_hist_words(nc) * 4, s));
     }
     if (st_ext) st = st_ext;
-    else { A(own_state.alloc(sizeof(GenState), pool, s)); st = own_state.as<GenState>(); }
+    else { take(own_state, sizeof(GenState)); st = own_state.as<GenState>(); }
     if (e != cudaSuccess) return e;
     A(cudaMemsetAsync(tally.p, 0, nb * 8, s)); A(cudaMemsetAsync(flux_acc.p, 0, nb * 8, s));
     A(cudaMemsetAsync(flux_sum.p, 0, nb * 8, s)); A(cudaMemsetAsync(flux_sq.p, 0, nb * 8, s));

@@ -93,9 +93,11 @@ struct InstBuffers {
     /* st_ext: a GenState slot owned by the caller, or nullptr to own one;
        pool: allocate stream-ordered on s from this pool (no device-wide
        synchronisation: the request server admits and retires many
-       instances), or nullptr for cudaMalloc */
+       instances), or nullptr for cudaMalloc; arena: small buffers from it
+       at 64 KB strides (batches) */
     cudaError_t alloc(uint64_t G_, uint64_t nc_, uint64_t gens_, uint64_t N, double bank_factor, bool bank,
-                      double k0, GenState* st_ext, cudaStream_t s, cudaMemPool_t pool = nullptr);
+                      double k0, GenState* st_ext, cudaStream_t s, cudaMemPool_t pool = nullptr,
+                      DeviceArena* arena = nullptr);
     EvBuffers view(uint64_t skip, uint64_t seed) const;
     uint64_t bytes() const;
 };

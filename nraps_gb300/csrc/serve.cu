@@ -94,6 +94,9 @@ int check_opts(nraps_ctx* ctx) {
 
 /* ======================================================================== */
 struct nraps_batch {
+    /* small buffers of the batch's instances and engine at 64 KB strides
+       (declared first: destroyed after every buffer it handed out) */
+    DeviceArena arena;
     nraps_ctx* ctx = nullptr;
     EventEngine ev;
     std::vector<std::unique_ptr<InstBuffers>> buf;
@@ -128,6 +131,7 @@ int nraps_batch_create(nraps_ctx* ctx, const nraps_problem* problems, uint32_t n
     std::unique_ptr<nraps_batch> b(new nraps_batch());
     b->ctx = ctx;
     std::string err;
+    b->ev.set_arena(&b->arena);
     if ((st = b->ev.configure(ctx->opts, err))) return set_err(ctx, st, err);
     /* one ranged pass (every particle to its end; each block a 4096-history
        range of one instance, its tables in shared memory): the fastest
@@ -163,7 +167,7 @@ int nraps_batch_create(nraps_ctx* ctx, const nraps_problem* problems, uint32_t n
         std::unique_ptr<InstBuffers> ib(new InstBuffers());
         cudaError_t e = ib->alloc(p.variables.energygroups, p.mesh.n_cells, p.variables.generations,
                                   p.variables.histories, ctx->opts.bank_factor, bank, (double)p.k_new, nullptr,
-                                  ctx->stream);
+                                  ctx->stream, nullptr, &b->arena);
         if (e != cudaSuccess) return set_err(ctx, nrint::cuda_status(e), std::string("batch buffers: ") + cudaGetErrorString(e));
         uint64_t seed = seeds ? seeds[i] : ctx->opts.seed + i;
         if (b->ev.add_instance(p, ib->view(p.variables.skip, seed), err) < 0)
