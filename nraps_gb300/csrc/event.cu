@@ -884,17 +884,18 @@ __device__ __forceinline__ void ev_pass_body(const EvArgs& a, int pass, uint32_t
     }
 }
 
-/* The transport kernels.  Registers: 56 for the persistent one-instance
-   transport (no spills; 9 blocks of 128 threads per SM instead of 8 measured
-   1-2% faster on single_large), 64 for ranged launches with the tables in
-   shared memory, 80 where table pointers are global (batched, ranged over
-   large tables). */
+/* The transport kernels.  Registers: 72 for the persistent one-instance
+   transport (no spills; 7 blocks of 128 threads per SM.  Measured on
+   single_large, 128-thread blocks, one launch per generation: 0.110 ms at a
+   cap of 48, 0.099 at 56, 0.095 at 64, 0.094 at 72, 0.095 at 80, 0.101 at
+   88 and 96), 64 for ranged launches with the tables in shared memory, 80
+   where table pointers are global (batched, ranged over large tables). */
 template <bool SOURCE, int ONE, bool EXACT, bool BANK, bool REC, bool OP>
 __global__ void __launch_bounds__(256, ONE == 2 ? 4 : 3) ev_pass(EvArgs a, int pass, uint32_t K, uint32_t tail) {
     ev_pass_body<SOURCE, ONE, EXACT, BANK, REC, OP>(a, pass, K, tail);
 }
 template <bool SOURCE, bool EXACT, bool BANK, bool REC, bool OP>
-__global__ void __maxnreg__(56) ev_pass_one(EvArgs a, int pass, uint32_t K, uint32_t tail) {
+__global__ void __maxnreg__(72) ev_pass_one(EvArgs a, int pass, uint32_t K, uint32_t tail) {
     ev_pass_body<SOURCE, 1, EXACT, BANK, REC, OP>(a, pass, K, tail);
 }
 /* ranged launches in 512-thread blocks (an autotuner candidate for batches:
