@@ -202,6 +202,10 @@ def measure_device(prob, arm: str, steps: int, warmup: int, seed: int, device: i
             flush.zero_()
             ev[i][0].record(ext)
         s.run(1)
+        if i == steps - 1:
+            # a generation's fold may run inside the next one's transport
+            # launch: the last one's goes inside the timed region too
+            s.flush()
         with torch.cuda.stream(ext):
             ev[i][1].record(ext)
     torch.cuda.synchronize(device)

@@ -243,9 +243,15 @@ int nraps_monte_carlo(nraps_ctx* ctx,
 int nraps_solve(nraps_ctx* ctx, const nraps_problem* problem, nraps_result* out);
 
 /* Device-resident session: tables and banks stay in HBM between calls.
-   run() enqueues generations on the context's stream and returns at once. */
+   run() enqueues generations on the context's stream and returns at once.
+   A WOODCOCK BANK session with one pass and few cells may leave the last
+   enqueued generation's fold (flux, fission source, entropy) pending: the
+   next generation's transport launch runs it, and sync(), results() and
+   timing() complete it first.  flush() enqueues it on the context's stream
+   without waiting (nothing when none is pending). */
 int  nraps_session_create(nraps_ctx* ctx, const nraps_problem* problem, nraps_session** out);
 int  nraps_session_run(nraps_session* s, uint64_t n_generations);
+int  nraps_session_flush(nraps_session* s);
 int  nraps_session_sync(nraps_session* s);
 int  nraps_session_results(nraps_session* s, nraps_result* out);
 /* Time each generation with CUDA events on the context's stream (turns CUDA

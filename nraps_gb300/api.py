@@ -63,6 +63,7 @@ def load(build_if_missing: bool = True):
     L.nraps_session_create.argtypes = [vp, P(abi.Problem), P(vp)]
     L.nraps_session_run.argtypes = [vp, C.c_uint64]
     L.nraps_session_sync.argtypes = [vp]
+    L.nraps_session_flush.argtypes = [vp]
     L.nraps_session_results.argtypes = [vp, P(abi.Result)]
     L.nraps_session_generation.argtypes = [vp]
     L.nraps_session_generation.restype = C.c_uint64
@@ -406,6 +407,10 @@ class Session:
 
     def run(self, n: int):
         _check(self._L.nraps_session_run(self.h, n), self.ctx.h)
+
+    def flush(self):
+        """Enqueue a pending fold of the last generation (no wait)."""
+        _check(self._L.nraps_session_flush(self.h), self.ctx.h)
 
     def sync(self):
         _check(self._L.nraps_session_sync(self.h), self.ctx.h)

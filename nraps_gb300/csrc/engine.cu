@@ -300,15 +300,22 @@ int create_session(nraps_ctx* ctx, const nraps_problem* p, bool with_records, nr
     CK(s->tables.alloc_in(s->arena, blob.size()));
     CK(cudaMemcpyAsync(s->tables.p, blob.data(), blob.size(), cudaMemcpyHostToDevice, sm));
     uint64_t nb = s->G * s->nc;
-    CK(s->tally.alloc_in(s->arena, nb * 8));
+    bool bank = s->o.mode == NRAPS_MODE_BANK;
+    bool woodcock = s->o.tracking == NRAPS_TRACK_WOODCOCK;
+    /* a Woodcock BANK session scores generation g into half g & 1 of a
+       two-half tally, so the event engine may fold a generation beside the
+       next one's transport (traces read one tally: they keep one) */
+    const uint64_t tally_halves = (woodcock && bank && !with_records) ? 2 : 1;
+    /* and keeps a small tally's bins one per 32 B sector */
+    const uint32_t tally_shift = (woodcock && !with_records) ? ev_tally_shift(nb) : 0u;
+    const uint64_t tally_words = tally_halves * (nb << tally_shift);
+    CK(s->tally.alloc_in(s->arena, tally_words * 8));
     CK(s->flux_acc.alloc_in(s->arena, nb * 8)); CK(s->flux_sum.alloc_in(s->arena, nb * 8)); CK(s->flux_sq.alloc_in(s->arena, nb * 8));
     CK(s->fs_acc.alloc_in(s->arena, s->nc * 8));
     CK(s->k64.alloc_in(s->arena, s->gens * 8)); CK(s->entropy.alloc_in(s->arena, s->gens * 8));
     CK(s->state.alloc_in(s->arena, sizeof(GenState)));
     uint32_t nfb = finalize_blocks_for(s->nc);
     CK(s->partials.alloc_in(s->arena, 2 * (size_t)nfb * 8));
-    bool bank = s->o.mode == NRAPS_MODE_BANK;
-    bool woodcock = s->o.tracking == NRAPS_TRACK_WOODCOCK;
     double bf = s->o.bank_factor > 0 ? s->o.bank_factor : 3.0;
     s->cap = bank ? (uint64_t)(bf * (double)s->N) + 1024 : 0;
     if (bank) {
@@ -328,7 +335,7 @@ int create_session(nraps_ctx* ctx, const nraps_problem* p, bool with_records, nr
         CK(s->records.alloc_in(s->arena, s->n_hist * sizeof(nraps_history_record)));
         CK(cudaMemsetAsync(s->records.p, 0, s->n_hist * sizeof(nraps_history_record), sm));
     }
-    CK(cudaMemsetAsync(s->tally.p, 0, nb * 8, sm));
+    CK(cudaMemsetAsync(s->tally.p, 0, tally_words * 8, sm));
     CK(cudaMemsetAsync(s->flux_acc.p, 0, nb * 8, sm));
     CK(cudaMemsetAsync(s->flux_sum.p, 0, nb * 8, sm));
     CK(cudaMemsetAsync(s->flux_sq.p, 0, nb * 8, sm));
@@ -395,6 +402,8 @@ int create_session(nraps_ctx* ctx, const nraps_problem* p, bool with_records, nr
         if (est) return set_err(ctx, est, e2);
         EvBuffers eb;
         eb.st = s->state.as<GenState>(); eb.tally = s->tally.as<double>();
+        eb.tally_shift = tally_shift;
+        eb.tally_stride = tally_halves == 2 ? nb << tally_shift : 0;
         eb.flux_acc = s->flux_acc.as<double>(); eb.fs_acc = s->fs_acc.as<double>();
         eb.flux_sum = s->flux_sum.as<double>(); eb.flux_sq = s->flux_sq.as<double>();
         eb.k64 = s->k64.as<double>(); eb.entropy = s->entropy.as<double>();
@@ -667,10 +676,25 @@ int nraps_session_run(nraps_session* s, uint64_t n) {
     return NRAPS_OK;
 }
 
+int nraps_session_flush(nraps_session* s) {
+    if (!s) return NRAPS_ERR_INVALID;
+    nraps_ctx* ctx = s->ctx;
+    cudaSetDevice(ctx->device);
+    if (s->ev) {
+        /* flux, fission source and entropy of a deferred last generation */
+        const int r = s->ev->flush_fold(ctx->stream);
+        if (r < 0) return set_err(ctx, NRAPS_ERR_CUDA, "fold flush launch failed");
+        ctx->launches += (uint64_t)r;
+    }
+    return NRAPS_OK;
+}
+
 int nraps_session_sync(nraps_session* s) {
     if (!s) return NRAPS_ERR_INVALID;
     nraps_ctx* ctx = s->ctx;
     cudaSetDevice(ctx->device);
+    const int fl = nraps_session_flush(s);
+    if (fl) return fl;
     CK(cudaStreamSynchronize(ctx->stream));
     for (size_t i = 0; i + 1 < s->tev.size(); i += 2) {
         float ms = 0.f;

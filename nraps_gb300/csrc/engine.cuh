@@ -45,6 +45,12 @@ struct GenState {
     /* k over the active generations so far: sum, sum of squares, count */
     double ksum, ksum2;
     unsigned long long nactive;
+    /* deferred end of generation (event engine, one instance): the
+       generation whose tallies and site histogram still wait to be folded
+       (by extra blocks of the next transport launch, or a flush), the k in
+       effect during it, its bank size and its entropy accumulator */
+    unsigned long long fold_pending, fold_gen, fold_B;
+    double fold_k, fold_h;
     unsigned long long pad2;
 };
 

@@ -100,6 +100,8 @@ struct EvInst {
     NDiv ndiv;                /* division by N                                 */
     GenState* st;
     double* tally;
+    uint64_t tally_stride;    /* generation g scores into tally + (g & 1) * this */
+    uint32_t tally_shift;     /* bin b of a half at [b << tally_shift]          */
     double *flux_acc, *fs_acc, *flux_sum, *flux_sq, *k64, *entropy;
     nraps_site* bank[2];
     uint64_t bank_cap;
@@ -123,6 +125,14 @@ struct EvArgs {
     unsigned long long* qcount;   /* MAX_PASSES+2: particles queued by pass p */
     unsigned long long* claim;    /* MAX_PASSES+2: input claimed by pass p    */
     unsigned long long* blocks_done; /* finalize: blocks that finished          */
+    /* deferred end of generation (one instance): blocks from fold_from on
+       of a one-pass transport launch fold the generation left pending
+       (0xFFFFFFFF: none); scatter_close: the last block of the bank scatter
+       closes the generation; their block counters */
+    uint32_t fold_from;
+    int scatter_close;
+    unsigned long long* scatter_done;
+    unsigned long long* fold_done;
     uint4* sites;                 /* NSLAB slabs of slab_cap site records      */
     unsigned long long* slab_count;
     uint64_t slab_cap;
@@ -257,15 +267,17 @@ struct Hot {
     uint32_t nc;
     float inv_k;                    /* (float)(1/k) of the previous generation */
     uint32_t inst;
-    uint32_t pad;
+    uint32_t tshift;                /* tally bin b at tally[b << tshift]       */
 };
 
 __device__ __forceinline__ void load_hot(Hot& h, const EvInst& I, uint32_t inst, bool bank) {
     const GenState* st = I.st;
-    h.tally = I.tally;
+    const uint64_t gen = st->gen;
+    h.tally = I.tally + (gen & 1) * I.tally_stride;
+    h.tshift = I.tally_shift;
     h.nc = I.nc;
     h.hist_begin = I.hist_begin;
-    h.gseed = nr_generation_seed(I.seed, st->gen);
+    h.gseed = nr_generation_seed(I.seed, gen);
     h.inv_k = bank ? st->inv_kf : 0.0f;
     h.inst = inst;
 }
@@ -759,7 +771,7 @@ __device__ __forceinline__ void ev_pass_body(const EvArgs& a, int pass, uint32_t
                         cell = __float_as_uint(rd.z) + k;
                         {
                             const Hot& h = s_hot[ONE ? 0 : threadIdx.x];
-                            nrdev::red_add_f64(&h.tally[(uint64_t)p.g * h.nc + cell], tv.inv_st64[j]);
+                            nrdev::red_add_f64(&h.tally[((uint64_t)p.g * h.nc + cell) << h.tshift], tv.inv_st64[j]);
                         }
                         unsigned long long q = tv.kq[j];
                         acc.kq += q;
@@ -894,8 +906,17 @@ template <bool SOURCE, int ONE, bool EXACT, bool BANK, bool REC, bool OP>
 __global__ void __launch_bounds__(256, ONE == 2 ? 4 : 3) ev_pass(EvArgs a, int pass, uint32_t K, uint32_t tail) {
     ev_pass_body<SOURCE, ONE, EXACT, BANK, REC, OP>(a, pass, K, tail);
 }
+__device__ __noinline__ void fold_pending_blocks(const EvArgs& a, uint32_t b, uint32_t nb);
 template <bool SOURCE, bool EXACT, bool BANK, bool REC, bool OP>
 __global__ void __maxnreg__(72) ev_pass_one(EvArgs a, int pass, uint32_t K, uint32_t tail) {
+    if (SOURCE && OP && BANK && !REC && blockIdx.x >= a.fold_from) {
+        /* a fold block: the blocks above the transport's are scheduled as
+           transport blocks leave their SMs */
+        nrdev::pdl_trigger();
+        nrdev::pdl_wait();
+        fold_pending_blocks(a, blockIdx.x - a.fold_from, gridDim.x - a.fold_from);
+        return;
+    }
     ev_pass_body<SOURCE, 1, EXACT, BANK, REC, OP>(a, pass, K, tail);
 }
 /* ranged launches in 512-thread blocks (an autotuner candidate for batches:
@@ -1082,7 +1103,7 @@ __global__ void __launch_bounds__(256) ev_sort_collide(EvArgs a, int round) {
     const uint64_t n_in = a.ccount[round];
     const int qout = round & 1;
     const float inv_k = BANK ? I.st->inv_kf : 0.0f;
-    double* tally = I.tally;
+    double* tally = I.tally + (I.st->gen & 1) * I.tally_stride;
     const uint32_t nc = I.nc;
     uint32_t staged_sites = 0;
     bool slab_full = false;
@@ -1112,7 +1133,7 @@ __global__ void __launch_bounds__(256) ev_sort_collide(EvArgs a, int round) {
             uint32_t k = rel > 0.0f ? (uint32_t)rel : 0u;
             if (k >= nr) k = nr - 1;
             cell = __float_as_uint(rd.z) + k;
-            nrdev::red_add_f64(&tally[(uint64_t)g * nc + cell], t.inv_st64[j]);
+            nrdev::red_add_f64(&tally[((uint64_t)g * nc + cell) << I.tally_shift], t.inv_st64[j]);
             acc.kq += t.kq[j];
             if (BANK) {
                 const float nu = __fadd_rn(__fmul_rn(X.z, inv_k), u24(nr_pcg32_next(&rng)));
@@ -1284,8 +1305,10 @@ __global__ void __launch_bounds__(256) ev_scatter(EvArgs a) {
    instead of thousands of same-address L2 atomics.  Four sites per thread are
    loaded before any is used, so each thread keeps four load chains
    (site -> parent offset) in flight. */
+__device__ __noinline__ void close_deferred(const EvArgs& a);
 __global__ void __launch_bounds__(SCATTER_ONE_THREADS) ev_scatter_hist(EvArgs a) {
     extern __shared__ uint32_t s_h[];
+    __shared__ bool s_last;
     nrdev::pdl_trigger();
     nrdev::pdl_wait();
     const uint32_t b = blockIdx.x;
@@ -1335,6 +1358,20 @@ __global__ void __launch_bounds__(SCATTER_ONE_THREADS) ev_scatter_hist(EvArgs a)
        per fuel cell instead of one per site */
     for (uint32_t c = threadIdx.x; c < nc; c += blockDim.x)
         if (s_h[c]) nrdev::red_add_u32(&I.hist[(uint64_t)c << I.hist_shift], s_h[c]);
+    if (a.scatter_close) {
+        /* deferred end of generation: the last block to finish (threadfence
+           + counter, no waiting) closes it */
+        __threadfence();
+        __syncthreads();
+        if (threadIdx.x == 0) s_last = atomicAdd(a.scatter_done, 1ULL) == gridDim.x - 1;
+        __syncthreads();
+        if (s_last) {
+            __threadfence();
+            close_deferred(a);
+            __syncthreads();
+            if (threadIdx.x == 0) *a.scatter_done = 0;
+        }
+    }
 }
 
 /* the instance of range r of a ranged launch (ranges of instance i are
@@ -1539,9 +1576,8 @@ __device__ __forceinline__ FoldK fold_factors(const EvInst& I, uint64_t gen, dou
  * another is issued before the first store: the work is a few L2 round
  * trips, not arithmetic.
  */
-__device__ __forceinline__ void fold_cell(const EvInst& I, uint64_t c, const FoldK& f) {
+__device__ __forceinline__ void fold_cell(const EvInst& I, double* __restrict__ tally, uint64_t c, const FoldK& f) {
     const uint32_t G = I.G, nc = I.nc;
-    double* __restrict__ tally = I.tally;
     double* __restrict__ flux_acc = I.flux_acc;
     double* __restrict__ flux_sum = I.flux_sum;
     double* __restrict__ flux_sq = I.flux_sq;
@@ -1560,7 +1596,7 @@ __device__ __forceinline__ void fold_cell(const EvInst& I, uint64_t c, const Fol
             const uint32_t g = g0 + u;
             const uint64_t bin = (uint64_t)g * nc + c;
             const bool ok = g < G;
-            tl[u] = ok ? tally[bin] : 0.0;
+            tl[u] = ok ? tally[bin << I.tally_shift] : 0.0;
             nsf[u] = ok ? I.nsf64[m + (uint64_t)I.M * g] : 0.0;
             fa[u] = (ok && active) ? flux_acc[bin] : 0.0;
             f1[u] = (ok && active) ? flux_sum[bin] : 0.0;
@@ -1571,7 +1607,7 @@ __device__ __forceinline__ void fold_cell(const EvInst& I, uint64_t c, const Fol
             const uint32_t g = g0 + u;
             if (g >= G) break;
             const uint64_t bin = (uint64_t)g * nc + c;
-            tally[bin] = 0.0;
+            tally[bin << I.tally_shift] = 0.0;
             fs += nsf[u] * (tl[u] * flux_scale);
             if (active) {
                 const double phi = tl[u] * phi_scale;
@@ -1585,13 +1621,15 @@ __device__ __forceinline__ void fold_cell(const EvInst& I, uint64_t c, const Fol
 }
 
 /* per-instance end of generation: k, entropy, bank size, counters */
-__device__ void finish_instance(const EvArgs& a, uint32_t i, const double* h_given = nullptr) {
+__device__ void finish_instance(const EvArgs& a, uint32_t i, const double* h_given = nullptr, bool defer = false) {
     const EvInst& I = a.inst[i];
     GenState* st = I.st;
-    /* every load first: this runs on one thread at the tail of the launch */
+    /* every load first: this runs on one thread at the tail of the launch
+       (h_acc is added to by other blocks: read past L1) */
     const uint64_t gen = st->gen;
     const unsigned long long kq = st->kq;
-    const double h = h_given ? *h_given : st->h_acc;
+    const double k_old = st->k;
+    const double h = h_given ? *h_given : *reinterpret_cast<volatile double*>(&st->h_acc);
     const double ksum = st->ksum, ksum2 = st->ksum2;
     const unsigned long long nactive = st->nactive, tot_sites = st->tot_sites, tot_hist = st->tot_histories;
     const unsigned int err0 = st->error;
@@ -1610,8 +1648,14 @@ __device__ void finish_instance(const EvArgs& a, uint32_t i, const double* h_giv
     if (gen >= I.skip) { st->ksum = ksum + k_new; st->ksum2 = ksum2 + k_new * k_new; st->nactive = nactive + 1; }
     unsigned int err = err0;
     if (a.bank) {
-        /* h holds -sum_c n_c log2(n_c) */
-        I.entropy[gen] = B ? nr_log((double)B) * LOG2E + h / (double)B : 0.0;
+        if (defer) {
+            /* flux, fission source and entropy of this generation are
+               folded later (fold_pending_blocks): keep what they need */
+            st->fold_gen = gen; st->fold_k = k_old; st->fold_B = B; st->fold_pending = 1;
+        } else {
+            /* h holds -sum_c n_c log2(n_c) */
+            I.entropy[gen] = B ? nr_log((double)B) * LOG2E + h / (double)B : 0.0;
+        }
         st->tot_sites = tot_sites + B;
         if (B > I.bank_cap) { B = I.bank_cap; err |= NR_ERR_CAPACITY; }
         st->n_bank = B;
@@ -1675,7 +1719,7 @@ __global__ void __launch_bounds__(FIN_THREADS) ev_finalize(EvArgs a) {
                 B = a.rb ? a.rb_total[inst] : a.offsets[I.hist_begin + I.N] - a.offsets[I.hist_begin];
             }
             if (gen < I.generations) {
-                fold_cell(I, c, a.n_inst == 1 ? s_f : fold_factors(I, gen, k));
+                fold_cell(I, I.tally + (gen & 1) * I.tally_stride, c, a.n_inst == 1 ? s_f : fold_factors(I, gen, k));
                 if (a.bank) {
                     I.hist[c << I.hist_shift] = 0;
                     if (cnt && B) h = -nlog2n(a, cnt);
@@ -1716,6 +1760,75 @@ __global__ void __launch_bounds__(FIN_THREADS) ev_finalize(EvArgs a) {
         }
         *a.blocks_done = 0;
     }
+}
+
+/*
+ * The deferred fold of instance 0: block b of nb folds cells
+ * b * blockDim + t, stepping by nb * blockDim, of the generation a deferred
+ * close left pending -- that generation's half of the tally into flux,
+ * flux moments and fission source (with the k in effect during it), and
+ * each cell's entropy term from the site histogram, which it clears.  The
+ * last block to finish writes the generation's entropy and clears the
+ * pending mark.  With nothing pending every block returns at once.
+ */
+__device__ __noinline__ void fold_pending_blocks(const EvArgs& a, uint32_t b, uint32_t nb) {
+    __shared__ FoldK s_f;
+    __shared__ unsigned long long s_gen, s_B;
+    __shared__ bool s_go, s_last;
+    const EvInst& I = a.inst[0];
+    GenState* st = I.st;
+    if (threadIdx.x == 0) {
+        const unsigned long long pend = st->fold_pending;
+        s_go = pend != 0;
+        if (pend) {
+            const uint64_t g = st->fold_gen;
+            s_gen = g;
+            s_B = st->fold_B;
+            s_f = fold_factors(I, g, st->fold_k);
+        }
+    }
+    __syncthreads();
+    if (!s_go) return;
+    const uint64_t g = s_gen, B = s_B;
+    double* tally = I.tally + (g & 1) * I.tally_stride;
+    double h = 0.0;
+    for (uint64_t c = (uint64_t)b * blockDim.x + threadIdx.x; c < I.nc; c += (uint64_t)nb * blockDim.x) {
+        fold_cell(I, tally, c, s_f);
+        uint32_t* hp = &I.hist[c << I.hist_shift];
+        const uint32_t cnt = *hp;
+        *hp = 0;
+        if (cnt && B) h -= nlog2n(a, cnt);
+    }
+    for (int o = 16; o > 0; o >>= 1) h += __shfl_down_sync(0xffffffffu, h, o);
+    if ((threadIdx.x & 31) == 0 && h != 0.0) atomicAdd(&st->fold_h, h);
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) s_last = atomicAdd(a.fold_done, 1ULL) == nb - 1;
+    __syncthreads();
+    if (!s_last || threadIdx.x != 0) return;
+    __threadfence();
+    /* added to by every block: read past L1 */
+    const double hs = *reinterpret_cast<volatile double*>(&st->fold_h);
+    I.entropy[g] = B ? nr_log((double)B) * LOG2E + hs / (double)B : 0.0;
+    st->fold_h = 0.0;
+    st->fold_pending = 0;
+    *a.fold_done = 0;
+}
+
+/* A flush of the deferred fold (before anything reads flux, fission source
+   or entropy, or a generation that closes the classic way) */
+__global__ void __launch_bounds__(FIN_THREADS) ev_fold_flush(EvArgs a) {
+    nrdev::pdl_trigger();
+    nrdev::pdl_wait();
+    fold_pending_blocks(a, blockIdx.x, gridDim.x);
+}
+
+/* The deferred close of instance 0, run by the last block of the bank
+   scatter: k, bank size, counters and generation index now (the next
+   transport needs them), the fold later */
+__device__ __noinline__ void close_deferred(const EvArgs& a) {
+    if (threadIdx.x == 0) finish_instance(a, 0, nullptr, true);
+    reset_pass_counters(a);
 }
 
 template <class T> struct DBuf {
@@ -1779,6 +1892,7 @@ struct EventEngine::Impl {
     nraps_history_record* rec = nullptr;
     EvArgs args{};
     bool committed = false;
+    bool fold_maybe_pending = false;   /* a deferred end of generation was enqueued */
     int grid_blocks = 0;
     /* sorted transport: the collision queue and the grid of its kernels */
     DBuf<float> cx, cmu;
@@ -1902,7 +2016,7 @@ int EventEngine::add_instance(const nraps_problem& p, const EvBuffers& b, std::s
     d.M = h.M; d.G = h.G; d.R = h.R; d.nc = h.nc; d.nbins = h.nbins; d.nfuel = h.nfuel;
     d.L = h.L; d.inv_binw = h.inv_binw; d.boundl = h.boundl; d.boundr = h.boundr;
     d.N = p.variables.histories; d.seed = b.seed; d.ndiv = NDiv::make(d.N);
-    d.st = b.st; d.tally = b.tally;
+    d.st = b.st; d.tally = b.tally; d.tally_stride = b.tally_stride; d.tally_shift = b.tally_shift;
     d.flux_acc = b.flux_acc; d.fs_acc = b.fs_acc; d.flux_sum = b.flux_sum; d.flux_sq = b.flux_sq;
     d.k64 = b.k64; d.entropy = b.entropy;
     d.bank[0] = b.bank[0]; d.bank[1] = b.bank[1]; d.bank_cap = b.bank_cap; d.hist = b.hist;
@@ -1966,9 +2080,11 @@ void set_smem_attr(size_t smem) {
     }
 }
 
+/* fold_blocks > 0 (one pass, one instance): that many blocks after the
+   transport's fold the generation a deferred close left pending */
 template <bool ONE, bool EXACT, bool BANK, bool REC>
 int launch_passes(const EvArgs& a, const EvParams& prm, int grid, size_t smem, uint64_t n_total,
-                  cudaStream_t s, bool pdl) {
+                  cudaStream_t s, bool pdl, uint32_t fold_blocks = 0) {
     int launched = 0;
     uint32_t block = prm.block;
     smem += stage_bytes(block);
@@ -1979,8 +2095,11 @@ int launch_passes(const EvArgs& a, const EvParams& prm, int grid, size_t smem, u
     if (P == 0) {
         /* one pass: every particle runs to its end */
         set_smem_attr<true, ONE, EXACT, BANK, REC, true>(smem);
-        e = launch_k(pdl, pass_kernel<true, ONE, EXACT, BANK, REC, true>(), dim3(g0), dim3(block), smem, s, a, 0,
-                     0xFFFFFFFFu, 0u);
+        EvArgs af = a;
+        if (ONE && BANK && !REC && fold_blocks) af.fold_from = g0;
+        else fold_blocks = 0;
+        e = launch_k(pdl, pass_kernel<true, ONE, EXACT, BANK, REC, true>(), dim3(g0 + fold_blocks), dim3(block), smem,
+                     s, af, 0, 0xFFFFFFFFu, 0u);
     } else {
         set_smem_attr<true, ONE, EXACT, BANK, REC, false>(smem);
         set_smem_attr<false, ONE, EXACT, BANK, REC, false>(smem);
@@ -2027,6 +2146,7 @@ void preload_kernels() {
     L((const void*)ev_sort_flight<false, EXACT, BANK>);
     L((const void*)ev_sort_collide<BANK>);
     L((const void*)ev_finalize);
+    L((const void*)ev_fold_flush);
     if (BANK) {
         L((const void*)ev_scatter_hist);
         L((const void*)ev_scatter<SCAT_ONE>);
@@ -2080,8 +2200,9 @@ int EventEngine::commit(cudaStream_t s, std::string& err) {
         A(m.block_sums.alloc((c + 4095) / 4096 + 1));
     }
     /* pass fills and claims, the finalize block count, the ranged bank's
-       chunk count, the sorted rounds' collision-queue fills */
-    constexpr size_t NCOUNT = 3 * (MAX_PASSES + 2) + 2;
+       chunk count, the sorted rounds' collision-queue fills, the deferred
+       close's and fold's block counts */
+    constexpr size_t NCOUNT = 3 * (MAX_PASSES + 2) + 4;
     if (!m.qcount.p) { A(m.qcount.alloc(NCOUNT)); A(m.slab_count.alloc(NSLAB)); A(m.bstats.alloc(1)); }
     /* slabs: room for every banked site plus one partial flush per warp */
     uint64_t want_slab = bank ? (bank_sum + 2 * m.n_total) / NSLAB + 8192 : 64;
@@ -2108,6 +2229,10 @@ int EventEngine::commit(cudaStream_t s, std::string& err) {
     a.rb = 0;
     a.rb_next = m.qcount.p + 2 * (MAX_PASSES + 2) + 1;
     a.ccount = m.qcount.p + 2 * (MAX_PASSES + 2) + 2;
+    a.scatter_done = m.qcount.p + 3 * (MAX_PASSES + 2) + 2;
+    a.fold_done = m.qcount.p + 3 * (MAX_PASSES + 2) + 3;
+    a.fold_from = 0xFFFFFFFFu;
+    a.scatter_close = 0;
     a.rb_pool_chunks = 0;
     a.rb_chunk = nullptr; a.rb_fill = nullptr; a.rb_base = nullptr; a.rb_total = nullptr;
     a.count = m.count.p; a.offsets = m.offsets.p;
@@ -2233,19 +2358,45 @@ uint64_t EventEngine::launches_per_generation() const {
     return params.passes == 0 ? 1 : 1 + params.passes;
 }
 
+int EventEngine::flush_fold(cudaStream_t s) {
+    Impl& m = *impl_;
+    if (!m.fold_maybe_pending) return 0;
+    const unsigned nb = (unsigned)std::max<uint64_t>(1, (m.inst[0]->d.nc + FIN_THREADS - 1) / FIN_THREADS);
+    if (launch_k(m.pdl, ev_fold_flush, dim3(nb), dim3(FIN_THREADS), 0, s, m.args) != cudaSuccess) return -1;
+    m.fold_maybe_pending = false;
+    return 1;
+}
+
 int EventEngine::enqueue_generation(cudaStream_t s, bool with_finalize, cudaEvent_t t0, cudaEvent_t t1) {
     Impl& m = *impl_;
     if (!m.committed) return -1;
     const EvArgs& a = m.args;
     bool bank = m.mode == NRAPS_MODE_BANK;
     bool rec = m.rec != nullptr;
+    const bool ranged_launch =
+        !rec && params.range && params.passes == 0 && m.range_built == params.range && (!bank || m.rb_ok);
+    /* deferred end of generation: one instance with a two-half tally, one
+       pass, cells counted in shared memory.  The scatter's last block closes
+       the generation and the next transport launch's extra blocks fold it. */
+    const bool deferred = with_finalize && a.hist_smem && !rec && !ranged_launch && params.passes == 0 &&
+                          !m.sort_grid && m.inst[0]->d.tally_stride != 0;
+    const uint32_t fold_blocks =
+        deferred ? (uint32_t)((m.inst[0]->d.nc + params.block - 1) / params.block) : 0u;
+    int n = 0;
+    if (!deferred && m.fold_maybe_pending) {
+        /* a generation that closes the classic way: fold the pending one first */
+        const int q = flush_fold(s);
+        if (q < 0) return -1;
+        n += q;
+    }
     /* arguments of the kernels after the transport (the ranged bank's
        buffers when a ranged launch uses it) */
     EvArgs ar = a;
     if (t0) cudaEventRecord(t0, s);
     int r;
 #define EV_LAUNCH(ONE, EXACT, BANK, REC) \
-    r = launch_passes<ONE, EXACT, BANK, REC>(a, params, m.grid_blocks, ONE ? m.smem_bytes : 0, m.n_total, s, m.pdl)
+    r = launch_passes<ONE, EXACT, BANK, REC>(a, params, m.grid_blocks, ONE ? m.smem_bytes : 0, m.n_total, s, m.pdl, \
+                                             fold_blocks)
     if (rec && m.one) {
         if (bank) { if (m.exact) EV_LAUNCH(true, true, true, true); else EV_LAUNCH(true, false, true, true); }
         else { if (m.exact) EV_LAUNCH(true, true, false, true); else EV_LAUNCH(true, false, false, true); }
@@ -2254,7 +2405,7 @@ int EventEngine::enqueue_generation(cudaStream_t s, bool with_finalize, cudaEven
            from global memory, as batched launches do */
         if (bank) { if (m.exact) EV_LAUNCH(false, true, true, true); else EV_LAUNCH(false, false, true, true); }
         else { if (m.exact) EV_LAUNCH(false, true, false, true); else EV_LAUNCH(false, false, false, true); }
-    } else if (params.range && params.passes == 0 && m.range_built == params.range && (!bank || m.rb_ok)) {
+    } else if (ranged_launch) {
         ar.range_len = params.range;
         ar.range_begin = m.d_range_begin.p;
         if (bank) {
@@ -2330,7 +2481,7 @@ int EventEngine::enqueue_generation(cudaStream_t s, bool with_finalize, cudaEven
 #undef EV_LAUNCH
     if (r < 0) return -1;
     if (t1) cudaEventRecord(t1, s);
-    int n = r;
+    n += r;
     if (bank && ar.rb) {
         launch_k(m.pdl, ev_rb_scan, dim3(a.n_inst), dim3(RB_THREADS), 0, s, ar);
         const size_t hb = ((size_t)ar.range_len + m.rb_hist_cells) * 4;
@@ -2345,7 +2496,9 @@ int EventEngine::enqueue_generation(cudaStream_t s, bool with_finalize, cudaEven
             const size_t hb = (size_t)m.inst[0]->d.nc * 4;
             if (hb > 40 * 1024)
                 cudaFuncSetAttribute(ev_scatter_hist, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hb);
-            launch_k(m.pdl, ev_scatter_hist, dim3(NSLAB * SCATTER_ONE_SPLIT), dim3(SCATTER_ONE_THREADS), hb, s, a);
+            EvArgs as = a;
+            as.scatter_close = deferred ? 1 : 0;
+            launch_k(m.pdl, ev_scatter_hist, dim3(NSLAB * SCATTER_ONE_SPLIT), dim3(SCATTER_ONE_THREADS), hb, s, as);
         } else if (m.one || rec) {
             launch_k(m.pdl, ev_scatter<SCAT_ONE>, dim3(NSLAB * 8), dim3(256), 0, s, a);
         } else if (a.n_inst <= SCAT_TAB_MAX) {
@@ -2355,7 +2508,8 @@ int EventEngine::enqueue_generation(cudaStream_t s, bool with_finalize, cudaEven
         }
         ++n;
     }
-    if (with_finalize) {
+    if (deferred) m.fold_maybe_pending = true;
+    if (with_finalize && !deferred) {
         unsigned gb = (unsigned)std::min<uint64_t>((m.n_cells_total + FIN_THREADS - 1) / FIN_THREADS,
                                                    (uint64_t)m.grid_blocks * 4);
         launch_k(m.pdl, ev_finalize, dim3(gb ? gb : 1), dim3(FIN_THREADS), 0, s, ar);

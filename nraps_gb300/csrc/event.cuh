@@ -16,6 +16,12 @@
  *               (ranged launches: each range orders its own sites);
  *   finalize    per-cell FP64 flux/fission-source accumulation, Shannon
  *               entropy, and per-instance k, bank size and generation index.
+ *               One instance with a two-half tally, one pass, few cells:
+ *               the last block of the bank scatter closes the generation (k,
+ *               bank size, generation index), and the fold (flux, fission
+ *               source, entropy) runs in extra blocks of the next transport
+ *               launch, which the SMs take up as the transport's last
+ *               histories leave them idle; a flush folds what is left.
  * Every particle owns a PCG32 stream (seed of its instance and generation,
  * stream = its history index within the instance), so the result does not
  * depend on K, P, the block size, or which other instances share the batch.
@@ -31,7 +37,14 @@
 /* Per-instance device buffers owned by the caller (a session or a batch). */
 struct EvBuffers {
     GenState* st;
-    double* tally;                         /* G*nc                          */
+    double* tally;                         /* G*nc, or two halves of G*nc   */
+    uint32_t tally_shift = 0;              /* bin b of a half at
+                                              tally[b << tally_shift]        */
+    uint64_t tally_stride = 0;             /* (G*nc) << tally_shift: generation
+                                              g scores into half g & 1 (the
+                                              fold of one generation can then
+                                              run beside the next one's
+                                              transport); 0: one tally      */
     double *flux_acc, *fs_acc, *flux_sum, *flux_sq;
     double *k64, *entropy;                 /* generations                    */
     nraps_site* bank[2];                   /* BANK mode ordered banks        */
@@ -49,6 +62,15 @@ struct EvBuffers {
 #define EV_HIST_SPREAD_MAX_CELLS 4096u
 __host__ __device__ inline uint32_t ev_hist_shift(uint64_t nc) { return nc <= EV_HIST_SPREAD_MAX_CELLS ? 5u : 0u; }
 __host__ __device__ inline uint64_t ev_hist_words(uint64_t nc) { return nc << ev_hist_shift(nc); }
+
+/* FP64 tally bins of a small instance one per 32 B sector (bin b at word
+   b << 2): with several bins to a sector the reductions of a launch queue on
+   fewer L2 sectors, and the transport's time depended on where the tally
+   lay (0.093-0.118 ms on a 2,000-cell, 4-group slab across 4 KB offsets;
+   flat at 0.092-0.093 ms spread out).  Larger tallies stay dense, so their
+   L2 footprint does not grow. */
+#define EV_TALLY_SPREAD_MAX_BINS 65536u
+__host__ __device__ inline uint32_t ev_tally_shift(uint64_t bins) { return bins <= EV_TALLY_SPREAD_MAX_BINS ? 2u : 0u; }
 
 struct EvParams {
     uint32_t block = 256;   /* threads per block of the transport passes       */
@@ -94,6 +116,11 @@ public:
     int enqueue_generation(cudaStream_t s, bool with_finalize = true, cudaEvent_t t0 = nullptr,
                            cudaEvent_t t1 = nullptr);
     uint64_t launches_per_generation() const;
+    /* Fold a generation left pending by a deferred end of generation (a
+       no-op launch-wise when none can be pending); returns kernels
+       launched, <0 on error.  Called before anything reads the flux,
+       fission source or entropy. */
+    int flush_fold(cudaStream_t s);
     /* Per-history records of instance 0 (trace), or nullptr. */
     void set_records(nraps_history_record* rec);
     /* Device scan offsets (n_total+1) of the last generation, for traces. */
