@@ -1359,14 +1359,16 @@ __global__ void __launch_bounds__(SCATTER_ONE_THREADS) ev_scatter_hist(EvArgs a)
     for (uint32_t c = threadIdx.x; c < nc; c += blockDim.x)
         if (s_h[c]) nrdev::red_add_u32(&I.hist[(uint64_t)c << I.hist_shift], s_h[c]);
     if (a.scatter_close) {
-        /* deferred end of generation: the last block to finish (threadfence
-           + counter, no waiting) closes it */
-        __threadfence();
+        /* deferred end of generation: the last block to finish (a counter,
+           no waiting) closes it.  No fence: the close reads only what
+           earlier launches wrote, and the one value of this launch it
+           overwrites -- the slab fills -- every block has read before its
+           increment (its loop bound depends on it); the bank and the
+           histogram are read by later launches. */
         __syncthreads();
         if (threadIdx.x == 0) s_last = atomicAdd(a.scatter_done, 1ULL) == gridDim.x - 1;
         __syncthreads();
         if (s_last) {
-            __threadfence();
             close_deferred(a);
             __syncthreads();
             if (threadIdx.x == 0) *a.scatter_done = 0;
