@@ -101,7 +101,9 @@ cudaError_t InstBuffers::alloc(uint64_t G_, uint64_t nc_, uint64_t gens_, uint64
     auto A = [&](cudaError_t x) { if (e == cudaSuccess) e = x; };
     /* small buffers at 64 KB strides from the arena, when there is one */
     auto take = [&](DevMem& d, size_t bytes) { A(arena ? d.alloc_in(*arena, bytes) : d.alloc(bytes, pool, s)); };
-    take(tally, nb * 8); take(flux_acc, nb * 8); take(flux_sum, nb * 8); take(flux_sq, nb * 8);
+    /* a small tally keeps its bins one per 32 B sector (see ev_tally_shift) */
+    tally_shift = ev_tally_shift(nb);
+    take(tally, (nb << tally_shift) * 8); take(flux_acc, nb * 8); take(flux_sum, nb * 8); take(flux_sq, nb * 8);
     take(fs_acc, nc * 8); take(k64, gens * 8); take(entropy, gens * 8);
     if (bank) {
         take(bank0, cap * sizeof(nraps_site)); take(bank1, cap * sizeof(nraps_site));
@@ -111,7 +113,7 @@ cudaError_t InstBuffers::alloc(uint64_t G_, uint64_t nc_, uint64_t gens_, uint64
     if (st_ext) st = st_ext;
     else { take(own_state, sizeof(GenState)); st = own_state.as<GenState>(); }
     if (e != cudaSuccess) return e;
-    A(cudaMemsetAsync(tally.p, 0, nb * 8, s)); A(cudaMemsetAsync(flux_acc.p, 0, nb * 8, s));
+    A(cudaMemsetAsync(tally.p, 0, (nb << tally_shift) * 8, s)); A(cudaMemsetAsync(flux_acc.p, 0, nb * 8, s));
     A(cudaMemsetAsync(flux_sum.p, 0, nb * 8, s)); A(cudaMemsetAsync(flux_sq.p, 0, nb * 8, s));
     A(cudaMemsetAsync(fs_acc.p, 0, nc * 8, s)); A(cudaMemsetAsync(k64.p, 0, gens * 8, s));
     A(cudaMemsetAsync(entropy.p, 0, gens * 8, s));
@@ -127,7 +129,7 @@ cudaError_t InstBuffers::alloc(uint64_t G_, uint64_t nc_, uint64_t gens_, uint64
 
 EvBuffers InstBuffers::view(uint64_t skip, uint64_t seed) const {
     EvBuffers b;
-    b.st = st; b.tally = tally.as<double>();
+    b.st = st; b.tally = tally.as<double>(); b.tally_shift = tally_shift;
     b.flux_acc = flux_acc.as<double>(); b.fs_acc = fs_acc.as<double>();
     b.flux_sum = flux_sum.as<double>(); b.flux_sq = flux_sq.as<double>();
     b.k64 = k64.as<double>(); b.entropy = entropy.as<double>();

@@ -90,6 +90,7 @@ struct InstBuffers {
     DevMem tally, flux_acc, flux_sum, flux_sq, fs_acc, k64, entropy, bank0, bank1, hist, own_state;
     GenState* st = nullptr;
     uint64_t G = 0, nc = 0, gens = 0, cap = 0;
+    uint32_t tally_shift = 0;     /* tally bin b at word b << tally_shift */
     /* st_ext: a GenState slot owned by the caller, or nullptr to own one;
        pool: allocate stream-ordered on s from this pool (no device-wide
        synchronisation: the request server admits and retires many
