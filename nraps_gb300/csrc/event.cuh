@@ -63,13 +63,14 @@ struct EvBuffers {
 __host__ __device__ inline uint32_t ev_hist_shift(uint64_t nc) { return nc <= EV_HIST_SPREAD_MAX_CELLS ? 5u : 0u; }
 __host__ __device__ inline uint64_t ev_hist_words(uint64_t nc) { return nc << ev_hist_shift(nc); }
 
-/* FP64 tally bins of a small instance one per 32 B sector (bin b at word
-   b << 2): with several bins to a sector the reductions of a launch queue on
-   fewer L2 sectors, and the transport's time depended on where the tally
-   lay (0.093-0.118 ms on a 2,000-cell, 4-group slab across 4 KB offsets;
-   flat at 0.092-0.093 ms spread out).  Larger tallies stay dense, so their
-   L2 footprint does not grow. */
-#define EV_TALLY_SPREAD_MAX_BINS 65536u
+/* FP64 tally bins one per 32 B sector (bin b at word b << 2): with several
+   bins to a sector the reductions of a launch queue on fewer L2 sectors.
+   On a 2,000-cell, 4-group slab the transport's time depended on where the
+   tally lay (0.093-0.118 ms across 4 KB offsets; flat at 0.092-0.093 ms
+   spread out); on a 200,000-cell, 8-group slab spreading took a generation
+   of 10M histories from 4.09 to 2.37 ms.  Tallies of more than 2M bins (64 MB
+   spread out, half the L2) stay dense. */
+#define EV_TALLY_SPREAD_MAX_BINS 2097152u
 __host__ __device__ inline uint32_t ev_tally_shift(uint64_t bins) { return bins <= EV_TALLY_SPREAD_MAX_BINS ? 2u : 0u; }
 
 struct EvParams {
