@@ -90,6 +90,8 @@ def test_event_graph_replay_equals_direct(ctx_factory):
     a = ctx_factory(use_graphs=1, **base).solve(p)
     b = ctx_factory(use_graphs=0, **base).solve(p)
     assert np.array_equal(a.k64, b.k64)
+    np.testing.assert_allclose(a.flux_mean, b.flux_mean, rtol=1e-11, atol=0)
+    np.testing.assert_allclose(a.entropy, b.entropy, rtol=0, atol=1e-12)
 
 
 def test_event_k_agrees_with_plain_fp64_bank(ctx_factory):
@@ -162,6 +164,11 @@ def test_autotuner_leaves_results_unchanged(ctx_factory):
     s.close()
     fixed = ctx_factory(events_per_pass=4, passes=3, block_size=256, **base).solve(p)
     assert np.array_equal(r.k64, fixed.k64)
+    # shapes that close a generation in the scatter and fold it in the next
+    # transport launch alternate with shapes that finalize in their own launch
+    np.testing.assert_allclose(r.flux_mean, fixed.flux_mean, rtol=1e-11, atol=0)
+    np.testing.assert_allclose(r.fission_source, fixed.fission_source, rtol=1e-6, atol=0)
+    np.testing.assert_allclose(r.entropy, fixed.entropy, rtol=0, atol=1e-12)
     assert len(t["tried_ms"]) == 12 and min(t["tried_ms"]) > 0
     assert t["block"] in (128, 256) and t["events_per_pass"] >= 1
     # one-pass shapes run every particle to its end (no queue passes)
