@@ -1443,6 +1443,8 @@ __global__ void __launch_bounds__(RB_THREADS) ev_rb_scan(EvArgs a) {
  * straight into the counters, one addition per distinct counter of a warp.
  */
 constexpr int RB_U = 4;
+/* shared-memory words of a range's padded count/offset array */
+__host__ __device__ constexpr uint32_t rb_loc_words(uint32_t range_len) { return range_len + range_len / 32 + 1; }
 __global__ void __launch_bounds__(RB_THREADS) ev_rb_scatter(EvArgs a) {
     extern __shared__ uint32_t s_rb[];           /* loc[range_len], hist[...] */
     constexpr uint32_t NW = RB_THREADS / 32;
@@ -1458,17 +1460,23 @@ __global__ void __launch_bounds__(RB_THREADS) ev_rb_scatter(EvArgs a) {
     const uint32_t nh = (uint32_t)((rb + a.range_len < iend ? rb + a.range_len : iend) - rb);
     const uint32_t nc = I.nc;
     const bool hsm = nc <= RB_HIST_SMEM;
+    /* loc: the range's per-history counts, then their exclusive scan, at
+       padded index j + j/32 (a thread's contiguous run below then reads
+       across the banks) */
     uint32_t* loc = s_rb;
-    uint32_t* hs = s_rb + a.range_len;
+    uint32_t* hs = s_rb + rb_loc_words(a.range_len);
     if (hsm)
         for (uint32_t c = threadIdx.x; c < nc; c += RB_THREADS) hs[c] = 0;
     for (uint32_t c = threadIdx.x; c < RB_MAXC; c += RB_THREADS) s_ck[c] = a.rb_chunk[(uint64_t)r * RB_MAXC + c];
+    /* the counts in one coalesced pass */
+    for (uint32_t j = threadIdx.x; j < nh; j += RB_THREADS) loc[j + (j >> 5)] = a.count[rb + j];
+    __syncthreads();
     /* exclusive scan of the range's site counts: each thread a contiguous
        run of ipt histories, then the block's run totals */
     const uint32_t ipt = (nh + RB_THREADS - 1) / RB_THREADS;
     const uint32_t j0 = threadIdx.x * ipt, j1 = j0 + ipt < nh ? j0 + ipt : nh;
     uint32_t sum = 0;
-    for (uint32_t j = j0; j < j1; ++j) sum += a.count[rb + j];
+    for (uint32_t j = j0; j < j1; ++j) sum += loc[j + (j >> 5)];
     uint32_t x = sum;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -1489,8 +1497,9 @@ __global__ void __launch_bounds__(RB_THREADS) ev_rb_scatter(EvArgs a) {
     __syncthreads();
     uint32_t run = (w ? s_w[w - 1] : 0u) + x - sum;
     for (uint32_t j = j0; j < j1; ++j) {
-        const uint32_t c = a.count[rb + j];
-        loc[j] = run;
+        const uint32_t jj = j + (j >> 5);
+        const uint32_t c = loc[jj];
+        loc[jj] = run;
         run += c;
     }
     __syncthreads();
@@ -1519,7 +1528,8 @@ __global__ void __launch_bounds__(RB_THREADS) ev_rb_scatter(EvArgs a) {
             bool w8 = ok[u] && parent >= rb && parent < rb + nh && cell < nc;
             uint64_t pos = 0;
             if (w8) {
-                pos = base + loc[parent - rb] + (v[u].w & 0xFFFFu);
+                const uint32_t jp = (uint32_t)(parent - rb);
+                pos = base + loc[jp + (jp >> 5)] + (v[u].w & 0xFFFFu);
                 w8 = pos < cap;
             }
             if (w8) out[pos] = make_uint4(v[u].x, cell, v[u].y >> 27, 0u);   /* nraps_site */
@@ -2486,7 +2496,7 @@ int EventEngine::enqueue_generation(cudaStream_t s, bool with_finalize, cudaEven
     n += r;
     if (bank && ar.rb) {
         launch_k(m.pdl, ev_rb_scan, dim3(a.n_inst), dim3(RB_THREADS), 0, s, ar);
-        const size_t hb = ((size_t)ar.range_len + m.rb_hist_cells) * 4;
+        const size_t hb = ((size_t)rb_loc_words(ar.range_len) + m.rb_hist_cells) * 4;
         if (hb > 40 * 1024) cudaFuncSetAttribute(ev_rb_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hb);
         launch_k(m.pdl, ev_rb_scatter, dim3(m.ranged_blocks), dim3(RB_THREADS), hb, s, ar);
         n += 2;
