@@ -29,6 +29,35 @@ constexpr int SCAN_THREADS = 1024;
 constexpr int SCAN_ITEMS = 4;
 constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
 static_assert(SCAN_TILE == (1 << NR_SCAN_TILE_LOG2), "scan tile size");
+static_assert(SCAN_ITEMS == 4, "a thread's items are one 16-byte vector");
+
+/* a thread's SCAN_ITEMS counts from `base` (a multiple of 4): one 16-byte
+   load when all lie below n and the array is 16-byte aligned (device
+   allocations are), else one by one with zeros past n */
+__device__ __forceinline__ uint4 load_items(const uint32_t* count, uint64_t n, uint64_t base) {
+    if (base + 3 < n && (reinterpret_cast<uintptr_t>(count) & 15u) == 0)
+        return reinterpret_cast<const uint4*>(count)[base >> 2];
+    uint4 v;
+    v.x = base < n ? count[base] : 0u;
+    v.y = base + 1 < n ? count[base + 1] : 0u;
+    v.z = base + 2 < n ? count[base + 2] : 0u;
+    v.w = base + 3 < n ? count[base + 3] : 0u;
+    return v;
+}
+
+/* the exclusive prefix of a thread's items, from `run`, to offsets[base..) */
+__device__ __forceinline__ void store_items(uint32_t* offsets, uint64_t n, uint64_t base, uint32_t run, uint4 v) {
+    uint4 o;
+    o.x = run; o.y = o.x + v.x; o.z = o.y + v.y; o.w = o.z + v.z;
+    if (base + 3 < n && (reinterpret_cast<uintptr_t>(offsets) & 15u) == 0) {
+        reinterpret_cast<uint4*>(offsets)[base >> 2] = o;
+        return;
+    }
+    if (base < n) offsets[base] = o.x;
+    if (base + 1 < n) offsets[base + 1] = o.y;
+    if (base + 2 < n) offsets[base + 2] = o.z;
+    if (base + 3 < n) offsets[base + 3] = o.w;
+}
 
 __global__ void __launch_bounds__(SCAN_THREADS) scan_tile_sums(const uint32_t* count, uint64_t n,
                                                                uint32_t* block_sums) {
@@ -36,8 +65,8 @@ __global__ void __launch_bounds__(SCAN_THREADS) scan_tile_sums(const uint32_t* c
     nrdev::pdl_trigger();
     nrdev::pdl_wait();
     uint64_t base = (uint64_t)blockIdx.x * SCAN_TILE + (uint64_t)threadIdx.x * SCAN_ITEMS;
-    uint32_t s = 0;
-    for (int i = 0; i < SCAN_ITEMS; ++i) if (base + i < n) s += count[base + i];
+    const uint4 v = load_items(count, n, base);
+    uint32_t s = v.x + v.y + v.z + v.w;
     uint32_t ex;
     uint32_t tot = block_excl_scan(s, &ex, sw);
     if (threadIdx.x == 0) block_sums[blockIdx.x] = tot;
@@ -69,16 +98,11 @@ __global__ void __launch_bounds__(SCAN_THREADS) scan_apply(const uint32_t* count
     nrdev::pdl_trigger();
     nrdev::pdl_wait();
     uint64_t base = (uint64_t)blockIdx.x * SCAN_TILE + (uint64_t)threadIdx.x * SCAN_ITEMS;
-    uint32_t v[SCAN_ITEMS];
-    uint32_t s = 0;
-    for (int i = 0; i < SCAN_ITEMS; ++i) { v[i] = (base + i < n) ? count[base + i] : 0u; s += v[i]; }
+    const uint4 v = load_items(count, n, base);
+    uint32_t s = v.x + v.y + v.z + v.w;
     uint32_t ex;
     block_excl_scan(s, &ex, sw);
-    uint32_t run = block_sums[blockIdx.x] + ex;
-    for (int i = 0; i < SCAN_ITEMS; ++i) {
-        if (base + i < n) offsets[base + i] = run;
-        run += v[i];
-    }
+    store_items(offsets, n, base, block_sums[blockIdx.x] + ex, v);
 }
 
 /* scan_top folded into scan_apply: each tile sums the tile totals before it
@@ -99,16 +123,11 @@ __global__ void __launch_bounds__(SCAN_THREADS) scan_apply_carry(const uint32_t*
     const uint32_t carry = block_excl_scan(c, &ex0, sw);
     __syncthreads();
     uint64_t base = (uint64_t)blockIdx.x * SCAN_TILE + (uint64_t)threadIdx.x * SCAN_ITEMS;
-    uint32_t v[SCAN_ITEMS];
-    uint32_t s = 0;
-    for (int i = 0; i < SCAN_ITEMS; ++i) { v[i] = (base + i < n) ? count[base + i] : 0u; s += v[i]; }
+    const uint4 v = load_items(count, n, base);
+    uint32_t s = v.x + v.y + v.z + v.w;
     uint32_t ex;
     const uint32_t tot = block_excl_scan(s, &ex, sw);
-    uint32_t run = carry + ex;
-    for (int i = 0; i < SCAN_ITEMS; ++i) {
-        if (base + i < n) offsets[base + i] = run;
-        run += v[i];
-    }
+    store_items(offsets, n, base, carry + ex, v);
     if (blockIdx.x == nb - 1 && threadIdx.x == 0) {
         offsets[n] = carry + tot;
         if (total) *total = carry + tot;
