@@ -338,17 +338,23 @@ def measure_plain_small(seed: int, device: int, threads: int):
     return out
 
 
-def measure_batched(seed: int, device: int, steps: int, warmup: int = 3):
+def measure_batched(seed: int, device: int, steps: int, warmup: int = 3, instances: int = 256, shape=None):
     """256 independent slabs (regions U{4..64}, groups U{2..8}, widths
     U[0.5,3] cm, histories log-uniform [10k,500k]) advancing together, one
-    CUDA-graph replay per generation."""
+    CUDA-graph replay per generation.  shape = (block, range_len) fixes the
+    launch shape (no autotuning: for profiling, where ncu's serialisation
+    would change the tuner's pick)."""
     import torch
     from nraps_gb300 import api, synth
-    # the batch's autotuner tries 12 launch shapes over its first inactive
-    # generations: warm up past them so the timed generations run the choice
-    warmup = max(warmup, 14)
-    probs = synth.batched(seed, n=256, inactive=max(20, warmup), active=max(20, steps))
-    ctx = api.Context(seed=seed, device=device, use_graphs=1, **ARMS["event"])
+    kw = dict(ARMS["event"])
+    if shape:
+        kw.update(block_size=shape[0], range_len=shape[1])
+    else:
+        # the batch's autotuner tries 12 launch shapes over its first inactive
+        # generations: warm up past them so the timed generations run the choice
+        warmup = max(warmup, 14)
+    probs = synth.batched(seed, n=instances, inactive=max(20, warmup), active=max(20, steps))
+    ctx = api.Context(seed=seed, device=device, use_graphs=1, **kw)
     b = api.Batch(ctx, probs, seeds=[seed * 1000 + i for i in range(len(probs))])
     b.run(warmup)
     tuning = b.tuning()
@@ -494,6 +500,10 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
     ap.add_argument("--batched-steps", type=int, default=10, help="timed generations of the 256-instance batch (0 = skip)")
+    ap.add_argument("--batched-instances", type=int, default=256, help="instances of the batch (profiling a smaller case)")
+    ap.add_argument("--batched-shape", type=str, default=None,
+                    help="BLOCK,RANGE_LEN: fix the batch's launch shape (no autotuning)")
+    ap.add_argument("--batched-warmup", type=int, default=3, help="untimed batch generations (at least 14 when autotuning)")
     ap.add_argument("--serve-seconds", type=float, default=60.0, help="Poisson arrival window of the serving run (config 3: 60 s; 0 = skip)")
     ap.add_argument("--serve-rate", type=float, default=200.0)
     ap.add_argument("--serve-sweep", default="400,800",
@@ -620,7 +630,9 @@ def main():
 
     small = (measure_plain_small(args.seed, local, max(1, (os.cpu_count() or 2) - 1))
              if args.plain_small and rank == 0 else None)
-    batched = measure_batched(args.seed, local, args.batched_steps) if args.batched_steps > 0 and arm == "event" else None
+    bshape = tuple(int(x) for x in args.batched_shape.split(",")) if args.batched_shape else None
+    batched = (measure_batched(args.seed, local, args.batched_steps, args.batched_warmup, args.batched_instances, bshape)
+               if args.batched_steps > 0 and arm == "event" else None)
     scale = measure_scale_stress(args.seed, local) if args.scale_stress and arm == "event" else None
     serving = (measure_serving(args.seed, local, args.serve_seconds, args.serve_rate)
                if args.serve_seconds > 0 and arm == "event" else None)
