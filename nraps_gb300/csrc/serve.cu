@@ -424,9 +424,11 @@ int nraps_server_submit(nraps_server* s, const nraps_problem* p, uint64_t seed, 
     uint64_t N = p->variables.histories, G = p->variables.energygroups, nc = p->mesh.n_cells;
     double bf = ctx->opts.bank_factor > 0 ? ctx->opts.bank_factor : 3.0;
     uint64_t cap = (uint64_t)(bf * (double)N) + 1024;
-    /* resident: tallies/accumulators, both banks, entropy counters, tables,
-       plus its share of the per-generation queues and site slabs */
-    r->bytes = G * nc * 8 * 4 + nc * 8 + 2 * cap * sizeof(nraps_site) + ev_hist_words(nc) * 4 +
+    /* resident: the tally (bins spread as InstBuffers lays them out),
+       flux accumulators, both banks, entropy counters, tables, plus its
+       share of the per-generation queues and site slabs */
+    r->bytes = ((G * nc) << ev_tally_shift(G * nc)) * 8 + G * nc * 8 * 3 + nc * 8 + 2 * cap * sizeof(nraps_site) +
+               ev_hist_words(nc) * 4 +
                EventEngine::table_bytes(*p) + N * (24 * 2 + 8) + (cap + 2 * N) * 16 + p->variables.generations * 16;
     std::lock_guard<std::mutex> lk(s->mu);
     if (r->bytes > s->o.hbm_budget_bytes) {
