@@ -56,11 +56,16 @@ struct EvBuffers {
 
 /* Site counters of the entropy histogram.  An instance with few cells keeps
    them 128 B apart (counter of cell c at word c << 5), so the additions to
-   its hot fuel cells spread over the L2 slices; a larger instance counts
-   densely, so its counters stay in L2 and neighbouring cells' additions
-   share sectors. */
+   its hot fuel cells spread over the L2 slices; up to 2M cells one counter
+   per 32 B sector (word c << 3: with eight to a sector, the additions of a
+   localised source's hot cells queued on a few sectors -- a 200,000-cell
+   slab's generation took 2.35 ms against 2.15 ms spread out); beyond that
+   densely. */
 #define EV_HIST_SPREAD_MAX_CELLS 4096u
-__host__ __device__ inline uint32_t ev_hist_shift(uint64_t nc) { return nc <= EV_HIST_SPREAD_MAX_CELLS ? 5u : 0u; }
+#define EV_HIST_SECTOR_MAX_CELLS 2097152u
+__host__ __device__ inline uint32_t ev_hist_shift(uint64_t nc) {
+    return nc <= EV_HIST_SPREAD_MAX_CELLS ? 5u : (nc <= EV_HIST_SECTOR_MAX_CELLS ? 3u : 0u);
+}
 __host__ __device__ inline uint64_t ev_hist_words(uint64_t nc) { return nc << ev_hist_shift(nc); }
 
 /* FP64 tally bins one per 32 B sector (bin b at word b << 2): with several
