@@ -1311,67 +1311,76 @@ __global__ void __launch_bounds__(SCATTER_ONE_THREADS) ev_scatter_hist(EvArgs a)
     __shared__ bool s_last;
     nrdev::pdl_trigger();
     nrdev::pdl_wait();
-    const uint32_t b = blockIdx.x;
     const EvInst& I = a.inst[0];
-    const uint32_t nc = I.nc;
-    for (uint32_t c = threadIdx.x; c < nc; c += blockDim.x) s_h[c] = 0;
-    const uint32_t slab = b / SCATTER_ONE_SPLIT, part = b % SCATTER_ONE_SPLIT;
-    uint64_t filled = a.slab_count[slab];
-    if (filled > a.slab_cap) filled = a.slab_cap;
-    /* this block's contiguous share of the slab */
-    const uint64_t per = (filled + SCATTER_ONE_SPLIT - 1) / SCATTER_ONE_SPLIT;
-    const uint64_t lo = per * part;
-    const uint64_t hi = lo + per < filled ? lo + per : filled;
-    const uint4* src = a.sites + (uint64_t)slab * a.slab_cap;
-    nraps_site* out = I.bank[(I.st->gen + 1) & 1];
-    const uint64_t cap = I.bank_cap;
-    __syncthreads();
-    constexpr int U = 4;
-    for (uint64_t j0 = lo + threadIdx.x; j0 < hi; j0 += (uint64_t)U * blockDim.x) {
-        uint4 v[U];
-        uint32_t off[U];
-        bool ok[U];
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-            uint64_t j = j0 + (uint64_t)u * blockDim.x;
-            ok[u] = j < hi;
-            v[u] = ok[u] ? src[j] : make_uint4(0, 0, 0, 0);
-            /* a slab that overflowed keeps stale records: never follow them */
-            ok[u] = ok[u] && v[u].z < a.n_total && (v[u].w >> 16) == 0u;
-        }
-#pragma unroll
-        for (int u = 0; u < U; ++u) off[u] = ok[u] ? a.offsets[v[u].z] : 0u;
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-            uint64_t pos = (uint64_t)off[u] + (v[u].w & 0xFFFFu);
-            if (ok[u] && pos < cap) {
-                uint32_t cell = v[u].y & 0x07FFFFFFu;
-                /* one 16-byte store (nraps_site is 4-byte aligned as a type;
-                   the bank itself is 256-byte aligned) */
-                reinterpret_cast<uint4*>(out)[pos] = make_uint4(v[u].x, cell, v[u].y >> 27, 0u);
-                if (cell < nc) atomicAdd(&s_h[cell], 1u);
+    if (a.scatter_close && blockIdx.x == gridDim.x - 1) {
+        /* deferred end of generation: the block after the scatter blocks
+           closes the generation while they scatter */
+        close_deferred(a);
+    } else {
+        const uint32_t b = blockIdx.x;
+        const uint32_t nc = I.nc;
+        for (uint32_t c = threadIdx.x; c < nc; c += blockDim.x) s_h[c] = 0;
+        const uint32_t slab = b / SCATTER_ONE_SPLIT, part = b % SCATTER_ONE_SPLIT;
+        uint64_t filled = a.slab_count[slab];
+        if (filled > a.slab_cap) filled = a.slab_cap;
+        /* this block's contiguous share of the slab */
+        const uint64_t per = (filled + SCATTER_ONE_SPLIT - 1) / SCATTER_ONE_SPLIT;
+        const uint64_t lo = per * part;
+        const uint64_t hi = lo + per < filled ? lo + per : filled;
+        const uint4* src = a.sites + (uint64_t)slab * a.slab_cap;
+        nraps_site* out = I.bank[(I.st->gen + 1) & 1];
+        const uint64_t cap = I.bank_cap;
+        __syncthreads();
+        constexpr int U = 4;
+        for (uint64_t j0 = lo + threadIdx.x; j0 < hi; j0 += (uint64_t)U * blockDim.x) {
+            uint4 v[U];
+            uint32_t off[U];
+            bool ok[U];
+    #pragma unroll
+            for (int u = 0; u < U; ++u) {
+                uint64_t j = j0 + (uint64_t)u * blockDim.x;
+                ok[u] = j < hi;
+                v[u] = ok[u] ? src[j] : make_uint4(0, 0, 0, 0);
+                /* a slab that overflowed keeps stale records: never follow them */
+                ok[u] = ok[u] && v[u].z < a.n_total && (v[u].w >> 16) == 0u;
+            }
+    #pragma unroll
+            for (int u = 0; u < U; ++u) off[u] = ok[u] ? a.offsets[v[u].z] : 0u;
+    #pragma unroll
+            for (int u = 0; u < U; ++u) {
+                uint64_t pos = (uint64_t)off[u] + (v[u].w & 0xFFFFu);
+                if (ok[u] && pos < cap) {
+                    uint32_t cell = v[u].y & 0x07FFFFFFu;
+                    /* one 16-byte store (nraps_site is 4-byte aligned as a type;
+                       the bank itself is 256-byte aligned) */
+                    reinterpret_cast<uint4*>(out)[pos] = make_uint4(v[u].x, cell, v[u].y >> 27, 0u);
+                    if (cell < nc) atomicAdd(&s_h[cell], 1u);
+                }
             }
         }
+        __syncthreads();
+        /* non-zero bins into the instance's counters: ~NSLAB additions
+           per fuel cell instead of one per site */
+        for (uint32_t c = threadIdx.x; c < nc; c += blockDim.x)
+            if (s_h[c]) nrdev::red_add_u32(&I.hist[(uint64_t)c << I.hist_shift], s_h[c]);
     }
-    __syncthreads();
-    /* non-zero bins into the instance's counters: ~NSLAB additions
-       per fuel cell instead of one per site */
-    for (uint32_t c = threadIdx.x; c < nc; c += blockDim.x)
-        if (s_h[c]) nrdev::red_add_u32(&I.hist[(uint64_t)c << I.hist_shift], s_h[c]);
     if (a.scatter_close) {
-        /* deferred end of generation: the last block to finish (a counter,
-           no waiting) closes it.  No fence: the close reads only what
-           earlier launches wrote, and the one value of this launch it
-           overwrites -- the slab fills -- every block has read before its
-           increment (its loop bound depends on it); the bank and the
-           histogram are read by later launches. */
+        /* the last block to finish (a counter, no waiting) advances the
+           generation index and clears the slab fills.  No fence: every
+           block read both before its increment (its loop bound and its
+           bank depend on them); the bank, the histogram and the close's
+           state are read by later launches. */
         __syncthreads();
         if (threadIdx.x == 0) s_last = atomicAdd(a.scatter_done, 1ULL) == gridDim.x - 1;
         __syncthreads();
         if (s_last) {
-            close_deferred(a);
-            __syncthreads();
-            if (threadIdx.x == 0) *a.scatter_done = 0;
+            for (uint32_t q = threadIdx.x; q < NSLAB; q += blockDim.x) a.slab_count[q] = 0;
+            if (threadIdx.x == 0) {
+                GenState* st = I.st;
+                const uint64_t g = st->gen;
+                if (g < I.generations) st->gen = g + 1;
+                *a.scatter_done = 0;
+            }
         }
     }
 }
@@ -1633,7 +1642,8 @@ __device__ __forceinline__ void fold_cell(const EvInst& I, double* __restrict__ 
 }
 
 /* per-instance end of generation: k, entropy, bank size, counters */
-__device__ void finish_instance(const EvArgs& a, uint32_t i, const double* h_given = nullptr, bool defer = false) {
+__device__ void finish_instance(const EvArgs& a, uint32_t i, const double* h_given = nullptr, bool defer = false,
+                                bool set_gen = true) {
     const EvInst& I = a.inst[i];
     GenState* st = I.st;
     /* every load first: this runs on one thread at the tail of the launch
@@ -1687,7 +1697,7 @@ __device__ void finish_instance(const EvArgs& a, uint32_t i, const double* h_giv
     st->n_sites = 0;
     st->k = k_new;
     st->inv_kf = (float)(1.0 / k_new);
-    st->gen = gen + 1;
+    if (set_gen) st->gen = gen + 1;
 }
 
 constexpr int FIN_THREADS = 64;
@@ -1835,12 +1845,16 @@ __global__ void __launch_bounds__(FIN_THREADS) ev_fold_flush(EvArgs a) {
     fold_pending_blocks(a, blockIdx.x, gridDim.x);
 }
 
-/* The deferred close of instance 0, run by the last block of the bank
-   scatter: k, bank size, counters and generation index now (the next
-   transport needs them), the fold later */
+/* The deferred close of instance 0, run by an extra block of the bank
+   scatter beside the scatter blocks: k, bank size, counters (what the next
+   transport needs; the fold comes later) -- all but the two values the
+   scatter blocks themselves read, the generation index and the slab fills,
+   which the scatter's last block advances and clears */
 __device__ __noinline__ void close_deferred(const EvArgs& a) {
-    if (threadIdx.x == 0) finish_instance(a, 0, nullptr, true);
-    reset_pass_counters(a);
+    if (threadIdx.x == 0) finish_instance(a, 0, nullptr, true, false);
+    for (uint32_t p = threadIdx.x; p < 2 * (MAX_PASSES + 2); p += blockDim.x) a.qcount[p] = 0;
+    for (uint32_t p = threadIdx.x; p < MAX_PASSES + 2; p += blockDim.x) a.ccount[p] = 0;
+    if (threadIdx.x == 0) *a.rb_next = 0;
 }
 
 template <class T> struct DBuf {
@@ -2510,7 +2524,8 @@ int EventEngine::enqueue_generation(cudaStream_t s, bool with_finalize, cudaEven
                 cudaFuncSetAttribute(ev_scatter_hist, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hb);
             EvArgs as = a;
             as.scatter_close = deferred ? 1 : 0;
-            launch_k(m.pdl, ev_scatter_hist, dim3(NSLAB * SCATTER_ONE_SPLIT), dim3(SCATTER_ONE_THREADS), hb, s, as);
+            launch_k(m.pdl, ev_scatter_hist, dim3(NSLAB * SCATTER_ONE_SPLIT + (deferred ? 1 : 0)),
+                     dim3(SCATTER_ONE_THREADS), hb, s, as);
         } else if (m.one || rec) {
             launch_k(m.pdl, ev_scatter<SCAT_ONE>, dim3(NSLAB * 8), dim3(256), 0, s, a);
         } else if (a.n_inst <= SCAT_TAB_MAX) {
