@@ -134,6 +134,23 @@ __global__ void __launch_bounds__(SCAN_THREADS) scan_apply_carry(const uint32_t*
     }
 }
 
+/* Per tile: the exclusive scan of its counts from the tile's start (local
+   offsets) and the tile's total.  A consumer that adds the tiles' bases
+   itself (an exclusive scan of the tile totals) gets the whole scan from
+   this one launch. */
+__global__ void __launch_bounds__(SCAN_THREADS) scan_local(const uint32_t* count, uint64_t n, uint32_t* tile_sums,
+                                                           uint32_t* offsets) {
+    __shared__ uint32_t sw[33];
+    nrdev::pdl_trigger();
+    nrdev::pdl_wait();
+    const uint64_t base = (uint64_t)blockIdx.x * SCAN_TILE + (uint64_t)threadIdx.x * SCAN_ITEMS;
+    const uint4 v = load_items(count, n, base);
+    uint32_t ex;
+    const uint32_t tot = block_excl_scan(v.x + v.y + v.z + v.w, &ex, sw);
+    store_items(offsets, n, base, ex, v);
+    if (threadIdx.x == 0) tile_sums[blockIdx.x] = tot;
+}
+
 __global__ void bank_scatter(BankArgs a) {
     const GenState* st = a.st;
     uint64_t n = st->n_sites;
@@ -262,6 +279,7 @@ void preload_bank_kernels() {
     cudaFuncGetAttributes(&fa, scan_top);
     cudaFuncGetAttributes(&fa, scan_apply);
     cudaFuncGetAttributes(&fa, scan_apply_carry);
+    cudaFuncGetAttributes(&fa, scan_local);
 }
 
 int launch_exclusive_scan(const uint32_t* count, uint64_t n, uint32_t* block_sums, uint32_t* offsets,
@@ -281,6 +299,16 @@ int launch_exclusive_scan(const uint32_t* count, uint64_t n, uint32_t* block_sum
             cudaSuccess)
         return -1;
     return 3;
+}
+
+int launch_scan_local(const uint32_t* count, uint64_t n, uint32_t* tile_sums, uint32_t* offsets, cudaStream_t s,
+                      bool pdl) {
+    const uint64_t nb = (n + SCAN_TILE - 1) / SCAN_TILE;
+    if (nb == 0) return 0;
+    if (launch_k(pdl, scan_local, dim3((unsigned)nb), dim3(SCAN_THREADS), 0, s, count, n, tile_sums, offsets) !=
+        cudaSuccess)
+        return -1;
+    return 1;
 }
 
 int launch_bank_order(const BankArgs& a, cudaStream_t s) {

@@ -153,6 +153,12 @@ int launch_exclusive_scan(const uint32_t* count, uint64_t n, uint32_t* block_sum
    NR_SCAN_CARRY_MAX_TILES tiles it takes two launches, beyond that three */
 constexpr int NR_SCAN_TILE_LOG2 = 12;
 constexpr uint64_t NR_SCAN_CARRY_MAX_TILES = 4096;
+/* per tile of 2^NR_SCAN_TILE_LOG2 counts: offsets relative to the tile's
+   start, and tile_sums[tile] = the tile's total (one launch; the consumer
+   adds the exclusive scan of tile_sums).  Returns launches (1, or 0 for
+   n = 0), or -1. */
+int launch_scan_local(const uint32_t* count, uint64_t n, uint32_t* tile_sums, uint32_t* offsets, cudaStream_t s,
+                      bool pdl = false);
 int launch_finalize(const FinalizeArgs& a, cudaStream_t s);
 int launch_pcg_stream(uint64_t seed, const uint64_t* streams, uint64_t n, uint32_t per,
                       uint32_t* out, cudaStream_t s);

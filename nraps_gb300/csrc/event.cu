@@ -45,6 +45,9 @@ constexpr uint32_t NSLAB = 128;
 constexpr uint32_t MAX_PASSES = 16;
 /* cells of a shared-memory site histogram in the single-instance scatter */
 constexpr uint32_t HIST_SMEM_MAX_CELLS = 12288;
+/* the scatter keeps the scan tiles' bases in shared memory beside the cell
+   histogram: up to this many tiles (33.5M histories) */
+constexpr uint64_t LOCAL_SCAN_MAX_TILES = 8192;
 /*
  * Unsigned division by an invariant divisor d (1 <= d < 2^63) as a 64x64
  * multiply-high, a subtraction and two shifts (Granlund & Montgomery,
@@ -138,6 +141,12 @@ struct EvArgs {
     uint64_t slab_cap;
     uint32_t* count;
     uint32_t* offsets;            /* n_total+1                                */
+    /* deferred end of generation: offsets hold each history's offset from
+       its scan tile's start, tile_sums the n_tiles tiles' totals (the scatter
+       adds the tiles' bases, the close takes the bank size from them);
+       nullptr: offsets are the whole exclusive scan */
+    uint32_t* tile_sums;
+    uint32_t n_tiles;
     GenState* stats;
     uint64_t max_events;
     nraps_history_record* rec;
@@ -1330,6 +1339,19 @@ __global__ void __launch_bounds__(SCATTER_ONE_THREADS) ev_scatter_hist(EvArgs a)
         const uint4* src = a.sites + (uint64_t)slab * a.slab_cap;
         nraps_site* out = I.bank[(I.st->gen + 1) & 1];
         const uint64_t cap = I.bank_cap;
+        /* offsets from the tiles' starts: the tiles' bases, an exclusive
+           scan of their totals, into shared memory after the histogram */
+        uint32_t* s_tb = s_h + nc;
+        if (a.tile_sums) {
+            __shared__ uint32_t s_sw[33];
+            const uint32_t T = a.n_tiles, per_t = (T + blockDim.x - 1) / blockDim.x;
+            const uint32_t t0 = threadIdx.x * per_t, t1 = t0 + per_t < T ? t0 + per_t : T;
+            uint32_t run = 0;
+            for (uint32_t t = t0; t < t1; ++t) run += a.tile_sums[t];
+            uint32_t ex;
+            nrdev::block_excl_scan(run, &ex, s_sw);
+            for (uint32_t t = t0; t < t1; ++t) { const uint32_t v = a.tile_sums[t]; s_tb[t] = ex; ex += v; }
+        }
         __syncthreads();
         constexpr int U = 4;
         for (uint64_t j0 = lo + threadIdx.x; j0 < hi; j0 += (uint64_t)U * blockDim.x) {
@@ -1345,7 +1367,8 @@ __global__ void __launch_bounds__(SCATTER_ONE_THREADS) ev_scatter_hist(EvArgs a)
                 ok[u] = ok[u] && v[u].z < a.n_total && (v[u].w >> 16) == 0u;
             }
     #pragma unroll
-            for (int u = 0; u < U; ++u) off[u] = ok[u] ? a.offsets[v[u].z] : 0u;
+            for (int u = 0; u < U; ++u)
+                off[u] = ok[u] ? a.offsets[v[u].z] + (a.tile_sums ? s_tb[v[u].z >> NR_SCAN_TILE_LOG2] : 0u) : 0u;
     #pragma unroll
             for (int u = 0; u < U; ++u) {
                 uint64_t pos = (uint64_t)off[u] + (v[u].w & 0xFFFFu);
@@ -1643,7 +1666,7 @@ __device__ __forceinline__ void fold_cell(const EvInst& I, double* __restrict__ 
 
 /* per-instance end of generation: k, entropy, bank size, counters */
 __device__ void finish_instance(const EvArgs& a, uint32_t i, const double* h_given = nullptr, bool defer = false,
-                                bool set_gen = true) {
+                                bool set_gen = true, const unsigned long long* b_given = nullptr) {
     const EvInst& I = a.inst[i];
     GenState* st = I.st;
     /* every load first: this runs on one thread at the tail of the launch
@@ -1656,7 +1679,8 @@ __device__ void finish_instance(const EvArgs& a, uint32_t i, const double* h_giv
     const unsigned long long nactive = st->nactive, tot_sites = st->tot_sites, tot_hist = st->tot_histories;
     const unsigned int err0 = st->error;
     unsigned long long B = 0;
-    if (a.bank) B = a.rb ? a.rb_total[i] : a.offsets[I.hist_begin + I.N] - a.offsets[I.hist_begin];
+    if (a.bank)
+        B = b_given ? *b_given : a.rb ? a.rb_total[i] : a.offsets[I.hist_begin + I.N] - a.offsets[I.hist_begin];
     unsigned long long c[5] = {0, 0, 0, 0, 0}, t[5] = {0, 0, 0, 0, 0};
     if (a.n_inst == 1) {
         c[0] = st->collisions; c[1] = st->virtual_collisions; c[2] = st->absorbed; c[3] = st->leaked;
@@ -1851,7 +1875,19 @@ __global__ void __launch_bounds__(FIN_THREADS) ev_fold_flush(EvArgs a) {
    scatter blocks themselves read, the generation index and the slab fills,
    which the scatter's last block advances and clears */
 __device__ __noinline__ void close_deferred(const EvArgs& a) {
-    if (threadIdx.x == 0) finish_instance(a, 0, nullptr, true, false);
+    __shared__ unsigned long long s_b[SCATTER_ONE_THREADS / 32];
+    unsigned long long B = 0;
+    if (a.tile_sums) {
+        /* the bank size: the sum of the scan tiles' totals */
+        unsigned long long t = 0;
+        for (uint32_t i = threadIdx.x; i < a.n_tiles; i += blockDim.x) t += a.tile_sums[i];
+        t = nrdev::warp_sum_u64(t);
+        if ((threadIdx.x & 31) == 0) s_b[threadIdx.x >> 5] = t;
+        __syncthreads();
+        if (threadIdx.x == 0)
+            for (uint32_t w = 0; w < (blockDim.x >> 5); ++w) B += s_b[w];
+    }
+    if (threadIdx.x == 0) finish_instance(a, 0, nullptr, true, false, a.tile_sums ? &B : nullptr);
     for (uint32_t p = threadIdx.x; p < 2 * (MAX_PASSES + 2); p += blockDim.x) a.qcount[p] = 0;
     for (uint32_t p = threadIdx.x; p < MAX_PASSES + 2; p += blockDim.x) a.ccount[p] = 0;
     if (threadIdx.x == 0) *a.rb_next = 0;
@@ -2261,7 +2297,7 @@ int EventEngine::commit(cudaStream_t s, std::string& err) {
     a.scatter_close = 0;
     a.rb_pool_chunks = 0;
     a.rb_chunk = nullptr; a.rb_fill = nullptr; a.rb_base = nullptr; a.rb_total = nullptr;
-    a.count = m.count.p; a.offsets = m.offsets.p;
+    a.count = m.count.p; a.offsets = m.offsets.p; a.tile_sums = nullptr; a.n_tiles = 0;
     a.stats = (n == 1) ? m.inst[0]->d.st : m.bstats.p;
     a.max_events = m.max_events;
     a.rec = m.rec;
@@ -2515,15 +2551,21 @@ int EventEngine::enqueue_generation(cudaStream_t s, bool with_finalize, cudaEven
         launch_k(m.pdl, ev_rb_scatter, dim3(m.ranged_blocks), dim3(RB_THREADS), hb, s, ar);
         n += 2;
     } else if (bank) {
-        int q = launch_exclusive_scan(m.count.p, m.n_total, m.block_sums.p, m.offsets.p, nullptr, s, m.pdl);
+        /* deferred end of generation: one scan launch of offsets within
+           tiles; the scatter adds the tiles' bases */
+        const uint64_t tiles = (m.n_total + (1ull << NR_SCAN_TILE_LOG2) - 1) >> NR_SCAN_TILE_LOG2;
+        const bool local = deferred && tiles <= LOCAL_SCAN_MAX_TILES;
+        int q = local ? launch_scan_local(m.count.p, m.n_total, m.block_sums.p, m.offsets.p, s, m.pdl)
+                      : launch_exclusive_scan(m.count.p, m.n_total, m.block_sums.p, m.offsets.p, nullptr, s, m.pdl);
         if (q < 0) return -1;
         n += q;
         if (a.hist_smem) {
-            const size_t hb = (size_t)m.inst[0]->d.nc * 4;
+            const size_t hb = ((size_t)m.inst[0]->d.nc + (local ? tiles : 0)) * 4;
             if (hb > 40 * 1024)
                 cudaFuncSetAttribute(ev_scatter_hist, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hb);
             EvArgs as = a;
             as.scatter_close = deferred ? 1 : 0;
+            if (local) { as.tile_sums = m.block_sums.p; as.n_tiles = (uint32_t)tiles; }
             launch_k(m.pdl, ev_scatter_hist, dim3(NSLAB * SCATTER_ONE_SPLIT + (deferred ? 1 : 0)),
                      dim3(SCATTER_ONE_THREADS), hb, s, as);
         } else if (m.one || rec) {
